@@ -1,0 +1,335 @@
+"""Benchmark of the k-means iteration hot path on GB300.
+
+Workload: Lloyd k-means, n = 1,048,576 points, d = 128, k = 256 (256 seeded
+isotropic Gaussian blobs, centers U[-10,10]^128, sigma = 1, FP32 input).  One
+step = one Lloyd iteration over all n points: distance stage with fused argmin,
+exact near-tie refinement, label sort (one-hot V), centroid update V.X,
+convergence and objective reductions.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision bf16|bf16x3|fp32]
+
+--impl ours (default) prints one JSON line: `value` = iterations/s of the
+BF16 tensor-core + exact-refinement path with the points resident in HBM
+(device-timed with CUDA events on the launching stream), the FP32 plain path
+beside it, labels compared between the two, `roofline` for the dominant kernel,
+`e2e` through the C ABI from pinned host memory, `cpu_baseline` (the oracle port
+on this host's cores).  --impl reference times the reference's CPU k-means
+algorithm on the host cores (the oracle port; the reference's own build where it
+exists) on a bounded sample per step.  N > 1 (torchrun) runs independent
+replicas, one per GPU ("replicas only": k-means here has no data-path exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "tests"))
+
+N, D, K = 1_048_576, 128, 256
+BLOBS, LO, HI, SIGMA, DATA_SEED = 256, -10.0, 10.0, 1.0, 1000
+KM_SEED, TOL = 0, 1e-4
+METRIC = "iters/s (n=1M,d=128,k=256): BF16-TC vs FP32 plain at equal labels; % of peak"
+LAUNCHES_PER_ITER = 9
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        j = json.loads(p.read_text())
+        return j["hbm_gbs"], j["bf16_tflops"], "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) >= 9:
+                for nm, v in zip(names, r[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def make_data(km):
+    return km.synth_blobs(N, D, BLOBS, LO, HI, SIGMA, DATA_SEED, nthreads=os.cpu_count() or 8)
+
+
+def run_cpu_sample(threads, sample_rows, reps=1, use_ref=False):
+    """The reference CPU k-means iteration (kmeans.cpp:86-148) on a bounded
+    sample: one assignment + update of `sample_rows` points against k=256
+    centroids on `threads` host threads (the oracle port), or the reference's own
+    build where it exists; scaled to iterations/s of the full n."""
+    import helpers
+    km = helpers.km()
+    X = km.synth_blobs(sample_rows, D, BLOBS, LO, HI, SIGMA, DATA_SEED, nthreads=threads)
+    rng = np.random.default_rng(0)
+    C0 = X[rng.choice(sample_rows, K, replace=False)].copy()
+    t = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        if use_ref:
+            helpers.ref_lloyd(X, K, -1.0, KM_SEED, 1)
+        else:
+            lab, _ = helpers.orc_assign(X, C0, threads=threads)
+            helpers.orc_update(X, lab, K, threads=threads)
+        t.append(time.perf_counter() - t0)
+    per_iter_full = min(t) * (N / sample_rows)
+    return 1.0 / per_iter_full, min(t)
+
+
+def reference_arm(args, rank):
+    import helpers
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    use_ref = helpers.reference_lib() is not None
+    if use_ref:
+        threads = 1                           # the reference CPU k-means is single-threaded
+    sample = 4096 if not use_ref else 2048
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, secs = run_cpu_sample(threads, sample, 1, use_ref)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    kind = "reference" if use_ref else "port"
+    line = {
+        "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": f"lloyd n={N} d={D} k={K} (256 gaussian blobs)", "n": N, "d": D, "k": K},
+        "cpu_baseline": {"value": value, "unit": "iters/s", "cores": threads, "kind": kind,
+                         "sample": f"one assignment+update of {sample} of the {N} points against k={K}"
+                                   f" centroids per step, scaled by n/{sample}"},
+        "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return line
+
+
+def ours_arm(args, rank, world):
+    import torch
+    import helpers
+    km = helpers.km()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()
+    X = make_data(km)
+    Xd = torch.from_numpy(X).to(f"cuda:{dev}")
+    res = {}
+    labels = {}
+    timing = {}
+    barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
+    with torch.cuda.stream(stream):
+        for prec in (args.precision, "fp32"):
+            m = km.Lloyd(N, D, K, tol=TOL, seed=KM_SEED, maxiter=args.warmup, precision=prec,
+                         conv="none", device=dev, stream=stream.cuda_stream).set_data(Xd)
+            m.fit(want_centroids=False)                         # warm-up iterations (graph built)
+            m.p.maxiter = args.steps
+            m.close()
+            m = km.Lloyd(N, D, K, tol=TOL, seed=KM_SEED, maxiter=args.steps, precision=prec,
+                         conv="none", device=dev, stream=stream.cuda_stream).set_data(Xd)
+            m.fit(want_centroids=False)                         # builds this handle's graph
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            barrier()
+            torch.cuda.synchronize()
+            clk = Clocks(dev)
+            with clk:
+                ev0.record(stream)
+                lab, _, r = m.fit(want_centroids=False)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+            barrier()
+            ms = ev0.elapsed_time(ev1)
+            # the fit above includes the seeded init; the library's own loop timer
+            # brackets exactly the `steps` iterations
+            timing[prec] = dict(ms_total=ms, ms_loop=r.fit_ms, iters=r.iterations, clocks=clk.summary(),
+                                refined=r.refined_rows, full=r.full_rescore_rows, objective=r.objective)
+            labels[prec] = lab
+            res[prec] = m
+    ms_loop = timing[args.precision]["ms_loop"]
+    if world > 1:
+        t = torch.tensor([ms_loop], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_loop = float(t.item())
+    iters = timing[args.precision]["iters"]
+    value = world * iters / (ms_loop / 1000.0)
+    fp32_ips = timing["fp32"]["iters"] / (timing["fp32"]["ms_loop"] / 1000.0)
+    agree = float((labels[args.precision] == labels["fp32"]).mean())
+
+    # per-stage timing with CUDA events on the launching stream
+    with torch.cuda.stream(stream):
+        stages = res[args.precision].profile(max(3, min(args.steps, 10)))
+        stages32 = res["fp32"].profile(3)
+    for m in res.values():
+        m.close()
+    names = ["distance+argmin", "refine", "label sort", "centroid sums", "finalize+control"]
+    hbm, bf16, src = peaks()
+    dp = (D + 63) // 64 * 64
+    # algorithmic bytes of each stage per iteration
+    bytes_stage = [N * dp * 2 + N * 4 + N * 4, 0, 3 * N * 4 + N * 4,
+                   N * D * 4 + N * 4 + 2 * K * D * 4, K * D * 4 * 3]
+    if args.precision == "bf16x3":
+        bytes_stage[0] += N * dp * 2
+    flops_dist = 2.0 * N * K * D
+    dom = int(np.argmax(stages))
+    st_ms = stages[dom]
+    if dom == 0:
+        ach_tf = flops_dist / (st_ms / 1e3) / 1e12
+        ach_gb = bytes_stage[0] / (st_ms / 1e3) / 1e9
+        # the distance GEMM sits at the ridge: report the tighter of the two bounds
+        if ach_gb / hbm >= ach_tf / bf16:
+            roof = {"bound": "hbm", "achieved": ach_gb, "peak": hbm, "unit": "GB/s", "frac": ach_gb / hbm}
+        else:
+            roof = {"bound": "tensor", "achieved": ach_tf, "peak": bf16, "unit": "TFLOP/s", "frac": ach_tf / bf16}
+    else:
+        ach_gb = bytes_stage[dom] / (st_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": ach_gb, "peak": hbm, "unit": "GB/s", "frac": ach_gb / hbm}
+    roof.update({"kernel": names[dom], "ms": st_ms, "peak_source": src,
+                 "traffic": TRAFFIC.get((args.precision, names[dom]))})
+
+    # e2e: the public C ABI from pinned host memory: set_data (H2D) + fit + labels D2H
+    e2e = None
+    if rank == 0 or world > 1:
+        Xp = torch.from_numpy(X).pin_memory()
+        with torch.cuda.stream(stream):
+            m = km.Lloyd(N, D, K, tol=TOL, seed=KM_SEED, maxiter=args.steps, precision=args.precision,
+                         conv="none", device=dev, stream=stream.cuda_stream)
+            import ctypes as C
+            lab = np.empty(N, np.uint32)
+            lab_p = torch.from_numpy(lab).pin_memory()
+            r = km.Result()
+            for rep in range(2):   # first call builds the graph
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                km.check(km.lib().km_lloyd_set_data(m.h, Xp.data_ptr(), 0), "set_data")
+                km.check(km.lib().km_lloyd_fit(m.h, None, lab_p.data_ptr(), None, C.byref(r)), "fit")
+                torch.cuda.synchronize()
+                wall = time.perf_counter() - t0
+            m.close()
+        e2e = {"value": r.iterations / wall, "unit": "iters/s", "h2d_bytes_per_step": N * D * 4,
+               "d2h_bytes_per_step": N * 4,
+               "step": f"one km_lloyd_fit from pinned host memory: km_lloyd_set_data (H2D of X) + "
+                       f"seeded init + {r.iterations} iterations + labels D2H; wall clock {wall * 1e3:.2f} ms"}
+
+    cpu = None
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        v, secs = run_cpu_sample(threads, 8192, 2)
+        cpu = {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
+               "sample": f"one assignment+update (oracle port of comparisons/CPU_Kmeans kmeans.cpp:86-148) "
+                         f"of 8192 of the {N} points against k={K}, {secs:.2f} s, scaled by n/8192"}
+    clocks = timing[args.precision]["clocks"]
+    line = {
+        "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_loop / iters, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if args.precision != "fp32" else "f32",
+        "data": "synthetic",
+        "config": {"workload": f"lloyd n={N} d={D} k={K} (256 gaussian blobs, sigma 1, centers U[-10,10])",
+                   "n": N, "d": D, "k": K, "precision": args.precision,
+                   "l2": "inputs larger than L2 (X fp32 512 MiB, bf16 256 MiB; L2 129 MB)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp32_plain": {"value": fp32_ips, "unit": "iters/s", "stages_ms": stages32},
+        "speedup_vs_fp32_plain": value / world / fp32_ips,
+        "label_agreement_vs_fp32": agree,
+        "refined_rows_per_iter": timing[args.precision]["refined"] / max(1, iters),
+        "full_rescore_rows_per_iter": timing[args.precision]["full"] / max(1, iters),
+        "objective": timing[args.precision]["objective"],
+        "stages_ms": dict(zip(names, stages)),
+        "roofline": roof,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": LAUNCHES_PER_ITER * iters,
+    }
+    return line
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum per launch from the committed ncu
+# summaries (profiles/); None until captured.
+TRAFFIC = {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "bf16x3", "fp32"])
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        line = reference_arm(args, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    line = ours_arm(args, rank, world)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,273 @@
+// Lloyd engine host code: buffers, preparation and the per-iteration launch
+// sequence (assign -> refine -> sort -> update -> finalize -> control).
+#include "km_lloyd.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+namespace km {
+
+namespace {
+thread_local std::string g_last_error;
+
+template <class T>
+km_status dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+  if (e != cudaSuccess) {
+    set_last_error(e, "cudaMalloc", __FILE__, __LINE__);
+    (void)cudaGetLastError();
+    return KM_ERR_ALLOC;
+  }
+  return KM_OK;
+}
+
+template <class T>
+void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+uint32_t round_up(uint32_t v, uint32_t m) { return (v + m - 1) / m * m; }
+}  // namespace
+
+void set_last_error(cudaError_t e, const char* what, const char* file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof buf, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+  g_last_error = buf;
+}
+
+const char* last_error_text() { return g_last_error.c_str(); }
+
+// Relative error coefficients of the fast distance path (see TieBound).
+TieBound make_tie_bound(int precision, uint32_t d) {
+  const double u = std::ldexp(1.0, -24);
+  const double ub = std::ldexp(1.0, -8);
+  const double uacc = std::ldexp(1.0, -22);  // tensor-core FP32 accumulation, 4 ulp per add
+  auto gamma = [](double m, double uu) { return m * uu / (1.0 - m * uu); };
+  double eps;
+  if (precision == KM_PREC_FP32) {
+    eps = gamma((double)d, u);
+  } else if (precision == KM_PREC_BF16) {
+    eps = 2 * ub + ub * ub + (1 + ub) * (1 + ub) * gamma((double)d, uacc);
+  } else {
+    eps = 3.5 * ub * ub + (1 + 5 * ub) * gamma(3.0 * d, uacc);
+  }
+  TieBound tb;
+  tb.A = (float)(2.02 * eps + 2.1 * u);
+  tb.B = (float)(2.1 * u);
+  tb.g = (float)(gamma((double)d + 2.0, u) * 1.01);
+  tb.safety = 1.25f;
+  return tb;
+}
+
+LloydEngine::~LloydEngine() {
+  if (device >= 0) cudaSetDevice(device);
+  dfree(X_owned); dfree(xn2); dfree(xn2d); dfree(Xb); dfree(Xlo);
+  dfree(C); dfree(Cn); dfree(cn2); dfree(dsq); dfree(objpart); dfree(shift_c); dfree(obj_c);
+  dfree(Cb); dfree(Clo); dfree(labels); dfree(mindist); dfree(queue);
+  dfree(seghist); dfree(counts); dfree(cstart); dfree(perm); dfree(red_part); dfree(st);
+  if (h_st) cudaFreeHost(h_st);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+km_status LloydEngine::init(uint64_t n_, uint32_t d_, uint32_t k_, int precision_, int device_,
+                            void* stream_, bool need_update) {
+  if (n_ == 0 || d_ == 0 || k_ == 0 || k_ > n_) return KM_ERR_ARG;
+  if (n_ >= (1ull << 32) - 256) return KM_ERR_ARG;           // labels / perm are 32-bit
+  if ((uint64_t)d_ * n_ / d_ != n_) return KM_ERR_ARG;
+  if (precision_ < KM_PREC_FP32 || precision_ > KM_PREC_BF16X3) return KM_ERR_ARG;
+  n = n_; d = d_; k = k_; precision = precision_; device = device_;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { (void)cudaGetLastError(); return KM_ERR_NO_DEVICE; }
+  if (device < 0 || device >= ndev) return KM_ERR_ARG;
+  KM_CUDA_TRY(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  KM_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+  if (prop.major != 10 || prop.minor != 3) return KM_ERR_NO_DEVICE;  // code is built for sm_103a only
+  num_sms = prop.multiProcessorCount;
+  if (stream_) {
+    stream = static_cast<cudaStream_t>(stream_);
+  } else {
+    KM_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    own_stream = true;
+  }
+  dp = round_up(d, 64);
+  kp = round_up(std::max<uint32_t>(k, 16), 16);
+  if (precision != KM_PREC_FP32) {
+    tc = plan_tc(dp, kp, precision == KM_PREC_BF16X3, n, num_sms);
+    if (!tc.ok) return KM_ERR_UNSUPPORTED;
+    KM_TRY(tc_set_attributes(tc, precision == KM_PREC_BF16X3));
+  }
+  tb = make_tie_bound(precision, d);
+
+  KM_TRY(dalloc(&xn2, n));
+  KM_TRY(dalloc(&xn2d, n));
+  if (precision != KM_PREC_FP32) {
+    KM_TRY(dalloc(&Xb, (size_t)n * dp));
+    KM_TRY(dalloc(&Cb, (size_t)kp * dp));
+    if (precision == KM_PREC_BF16X3) {
+      KM_TRY(dalloc(&Xlo, (size_t)n * dp));
+      KM_TRY(dalloc(&Clo, (size_t)kp * dp));
+    }
+  }
+  KM_TRY(dalloc(&C, (size_t)k * d));
+  KM_TRY(dalloc(&cn2, kp));
+  KM_TRY(dalloc(&labels, n));
+  KM_TRY(dalloc(&mindist, n));
+  KM_TRY(dalloc(&queue, n));
+  KM_TRY(dalloc(&red_part, 256));
+  KM_TRY(dalloc(&st, 1));
+  KM_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&h_st), sizeof(DevState)));
+  std::memset(h_st, 0, sizeof(DevState));
+  KM_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(DevState), stream));
+
+  // Stable-sort geometry: segments of `seg` rows, k x nseg counts.
+  seg = 1024;
+  nseg = (uint32_t)((n + seg - 1) / seg);
+  while ((uint64_t)k * nseg > (16ull << 20) && seg < (1u << 30)) {
+    seg <<= 1;
+    nseg = (uint32_t)((n + seg - 1) / seg);
+  }
+  const size_t per_warp = (size_t)k * 4;
+  if (per_warp <= 6144) sort_wpb = 8;
+  else sort_wpb = (int)std::max<size_t>(1, (48 * 1024) / per_warp);
+  sort_smem = per_warp * sort_wpb;
+  if (sort_smem > 227 * 1024) return KM_ERR_UNSUPPORTED;
+  if (sort_smem > 48 * 1024) {
+    KM_CUDA_TRY(cudaFuncSetAttribute(seg_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem));
+    KM_CUDA_TRY(cudaFuncSetAttribute(seg_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem));
+  }
+  if (need_update) {
+    KM_TRY(dalloc(&Cn, (size_t)k * d));
+    KM_TRY(dalloc(&dsq, (size_t)k * d));
+    KM_TRY(dalloc(&objpart, (size_t)k * d));
+    KM_TRY(dalloc(&shift_c, k));
+    KM_TRY(dalloc(&obj_c, k));
+    KM_TRY(dalloc(&seghist, (size_t)k * nseg));
+    KM_TRY(dalloc(&counts, k));
+    KM_TRY(dalloc(&cstart, (size_t)k + 1));
+    KM_TRY(dalloc(&perm, n));
+  }
+  return KM_OK;
+}
+
+km_status LloydEngine::set_points(const float* Xsrc, bool on_device, bool copy) {
+  KM_CUDA_TRY(cudaSetDevice(device));
+  if (copy || !on_device) {
+    if (!X_owned) KM_TRY(dalloc(&X_owned, (size_t)n * d));
+    KM_CUDA_TRY(cudaMemcpyAsync(X_owned, Xsrc, sizeof(float) * n * d,
+                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
+    X = X_owned;
+  } else {
+    X = Xsrc;
+  }
+  KM_CUDA_TRY(cudaMemsetAsync(&st->err, 0, sizeof(uint32_t), stream));
+  const int blocks = (int)std::min<uint64_t>((n + 7) / 8, (uint64_t)num_sms * 16);
+  prep_points_kernel<<<blocks, 256, 0, stream>>>(X, n, d, dp, xn2, xn2d, Xb, Xlo, st);
+  KM_CUDA_TRY(cudaGetLastError());
+  reduce_f64_partial_kernel<<<256, 256, 0, stream>>>(xn2d, n, red_part);
+  reduce_f64_final_kernel<<<1, 32, 0, stream>>>(red_part, 256, &st->sum_x2);
+  KM_CUDA_TRY(cudaGetLastError());
+  if (precision != KM_PREC_FP32) {
+    KM_TRY(encode_tmap_bf16(&tmA, Xb, dp, n, 64, 128));
+    KM_TRY(encode_tmap_bf16(&tmB, Cb, dp, kp, 64, kp));
+    if (precision == KM_PREC_BF16X3) {
+      KM_TRY(encode_tmap_bf16(&tmAlo, Xlo, dp, n, 64, 128));
+      KM_TRY(encode_tmap_bf16(&tmBlo, Clo, dp, kp, 64, kp));
+    } else {
+      tmAlo = tmA;
+      tmBlo = tmB;
+    }
+  }
+  KM_TRY(read_state());
+  if (h_st->err & KM_DEVERR_NONFINITE) return KM_ERR_ARG;
+  data_ready = true;
+  return KM_OK;
+}
+
+km_status LloydEngine::reset_state() {
+  // Keep sum_x2 (computed at set_points); zero everything else.
+  KM_TRY(read_state());
+  const double sx = h_st->sum_x2;
+  std::memset(h_st, 0, sizeof(DevState));
+  h_st->sum_x2 = sx;
+  KM_CUDA_TRY(cudaMemcpyAsync(st, h_st, sizeof(DevState), cudaMemcpyHostToDevice, stream));
+  KM_CUDA_TRY(cudaStreamSynchronize(stream));
+  return KM_OK;
+}
+
+km_status LloydEngine::set_centroids_dev(const float* Csrc) {
+  if (Csrc != C)
+    KM_CUDA_TRY(cudaMemcpyAsync(C, Csrc, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
+  KM_CUDA_TRY(cudaMemsetAsync(&st->cmax, 0, sizeof(float), stream));
+  const int blocks = (int)((kp * 32 + 255) / 256);
+  prep_centroids_kernel<<<blocks, 256, 0, stream>>>(C, k, kp, d, dp, cn2, Cb, Clo, st);
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
+
+km_status LloydEngine::enqueue_assign(float* Dout) {
+  if (precision == KM_PREC_FP32) {
+    const unsigned blocks = (unsigned)((n + 127) / 128);
+    assign_f32_kernel<<<blocks, 256, 0, stream>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
+                                                  queue, Dout);
+    KM_CUDA_TRY(cudaGetLastError());
+  } else {
+    KM_TRY(launch_assign_tc(tc, precision == KM_PREC_BF16X3, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k,
+                            kp, tb, st, labels, mindist, queue, Dout, stream));
+  }
+  refine_kernel<<<num_sms * 4, 256, 0, stream>>>(X, C, d, k, st, queue, labels, mindist);
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
+
+km_status LloydEngine::enqueue_sort(const uint32_t* lab) {
+  const unsigned hb = (nseg + sort_wpb - 1) / sort_wpb;
+  seg_hist_kernel<<<hb, sort_wpb * 32, sort_smem, stream>>>(lab, n, k, seg, nseg, seghist, st);
+  seg_scan_kernel<<<(k * 32 + 255) / 256, 256, 0, stream>>>(seghist, k, nseg, counts, st);
+  cluster_scan_kernel<<<1, 1024, 0, stream>>>(counts, k, cstart, st);
+  seg_scatter_kernel<<<hb, sort_wpb * 32, sort_smem, stream>>>(lab, n, k, seg, nseg, seghist, cstart,
+                                                               perm, st);
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
+
+km_status LloydEngine::enqueue_update_step(float tol) {
+  const uint64_t pairs = (uint64_t)k * d;
+  update_sums_kernel<<<(unsigned)((pairs + 127) / 128), 128, 0, stream>>>(X, perm, cstart, d, k, C, Cn,
+                                                                          dsq, objpart, st);
+  finalize_kernel<<<(k * 32 + 255) / 256, 256, 0, stream>>>(Cn, C, dsq, objpart, d, dp, k, tol, cn2,
+                                                            Cb, Clo, shift_c, obj_c, st);
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
+
+km_status LloydEngine::enqueue_iteration(const LoopConsts& lc) {
+  KM_TRY(enqueue_assign(nullptr));
+  KM_TRY(enqueue_sort(labels));
+  KM_TRY(enqueue_update_step(lc.tol));
+  control_kernel<<<1, 256, 0, stream>>>(cn2, shift_c, obj_c, k, lc, st);
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
+
+km_status LloydEngine::read_state() {
+  KM_CUDA_TRY(cudaMemcpyAsync(h_st, st, sizeof(DevState), cudaMemcpyDeviceToHost, stream));
+  KM_CUDA_TRY(cudaStreamSynchronize(stream));
+  return KM_OK;
+}
+
+km_status LloydEngine::check_device_error() {
+  KM_TRY(read_state());
+  if (h_st->err & KM_DEVERR_TIMEOUT) return KM_ERR_TIMEOUT;
+  if (h_st->err & KM_DEVERR_NONFINITE) return KM_ERR_ARG;
+  if (h_st->err & KM_DEVERR_OVERFLOW) return KM_ERR_ARG;
+  return KM_OK;
+}
+
+}  // namespace km

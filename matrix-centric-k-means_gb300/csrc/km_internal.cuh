@@ -1,0 +1,339 @@
+// Internal definitions shared by the libkm_sm103 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/km.h"
+
+namespace km {
+
+// ---------------------------------------------------------------------------
+// Host-side error plumbing: every CUDA call maps to a km_status; nothing exits.
+// ---------------------------------------------------------------------------
+#define KM_CUDA_TRY(expr)                                                        \
+  do {                                                                           \
+    cudaError_t _e = (expr);                                                     \
+    if (_e != cudaSuccess) {                                                     \
+      km::set_last_error(_e, #expr, __FILE__, __LINE__);                         \
+      return (_e == cudaErrorMemoryAllocation) ? KM_ERR_ALLOC : KM_ERR_CUDA;     \
+    }                                                                            \
+  } while (0)
+
+#define KM_TRY(expr)                          \
+  do {                                        \
+    km_status _s = (expr);                    \
+    if (_s != KM_OK) return _s;               \
+  } while (0)
+
+void set_last_error(cudaError_t e, const char* what, const char* file, int line);
+
+// ---------------------------------------------------------------------------
+// Device-resident loop state of one fit.  Every per-iteration kernel reads
+// `done` first and returns when it is set, so iterations enqueued past the stop
+// cost one empty launch each and no host synchronisation is needed per
+// iteration.
+// ---------------------------------------------------------------------------
+struct DevState {
+  uint32_t done;            // fit finished (stop rule fired or maxiter reached)
+  uint32_t iter;            // iterations executed
+  uint32_t converged_iter;  // iteration at which the stop rule fired (0: not yet)
+  uint32_t moved;           // some centroid moved more than tol in this iteration
+  uint32_t flag_count;      // rows queued for near-tie refinement in this iteration
+  uint32_t err;             // device error bits (KM_DEVERR_*)
+  uint32_t err_where;       // first wait that ran out (diagnostics)
+  uint32_t pad0;
+  unsigned long long refined_total;
+  unsigned long long full_total;
+  float cmax;               // max_c ||c|| of the centroids the next assignment uses
+  float pad1;
+  double objective;         // FP64 objective of the last assignment
+  double last_score;
+  double score;
+  double max_shift;
+  double sum_x2;            // FP64 sum_i ||x_i||^2
+};
+
+enum : uint32_t {
+  KM_DEVERR_TIMEOUT = 1u,   // a bounded wait ran out
+  KM_DEVERR_NONFINITE = 2u, // input held NaN/Inf
+  KM_DEVERR_OVERFLOW = 4u   // refinement list overflow (cannot happen: list holds n)
+};
+
+// Per-fit constants passed by value to the control kernel.
+struct LoopConsts {
+  uint64_t maxiter;
+  float tol;
+  int32_t conv;       // km_conv
+};
+
+// ---------------------------------------------------------------------------
+// Near-tie bound.  A fast-path distance is v(c) = fl(||c||^2 - 2 * dot(x, c)),
+// with |v(c) - (||c||^2 - 2 x.c)| <= E(c) = A*||x||*||c|| + B*||c||^2, where
+// A = 2*eps_dot + 2u covers the dot-product error and the final rounding and
+// B = 2u covers the rounding of ||c||^2 and of the subtraction.  The
+// reference's CPU distance sum_j fl(fl(x_j - c_j)^2), summed in float, has
+// relative error at most g = gamma_{d+2}.  If, with T an upper bound of
+// ||x||^2, v1 <= v2 <= v3 the three smallest fast values and c1 the argmin,
+//   (v2 - v1) > Emax + E1 + g * (2T + v1 + v2 + E1 - Emax)
+// then the reference's argmin is c1 (class 0).  The same test with v3 in place
+// of v2 proves it is one of the two best fast candidates (class 1); otherwise
+// the row is re-scored against all k centroids (class 2).  Both refinements use
+// the reference's exact formula, so the final labels equal the reference's.
+// ---------------------------------------------------------------------------
+struct TieBound {
+  float A;      // coefficient of ||x||*||c||
+  float B;      // coefficient of ||c||^2
+  float g;      // relative error of the reference CPU distance
+  float safety; // multiplier on the right-hand side (covers this test's own rounding)
+};
+
+TieBound make_tie_bound(int precision, uint32_t d);
+
+__device__ __forceinline__ int tie_class(float X2, float v1, float v2, float v3, float cn1,
+                                         float cmax, const TieBound& tb) {
+  const float nx = sqrtf(X2) * 1.0000005f;
+  const float T = X2 * 1.0000003f;
+  const float E1 = tb.A * nx * cn1 + tb.B * cn1 * cn1;
+  const float Em = tb.A * nx * cmax + tb.B * cmax * cmax;
+  const float base = Em + E1;
+  const float s = fmaxf(0.0f, 2.0f * T + v1 + E1 - Em);
+  const float rhs2 = tb.safety * (base + tb.g * (s + v2)) + 1e-30f;
+  const float rhs3 = tb.safety * (base + tb.g * (s + v3)) + 1e-30f;
+  // NaN or Inf anywhere makes the comparisons false: such rows take the full path.
+  const bool fin = isfinite(T + v1 + E1 + Em);
+  if (fin && (v2 - v1) > rhs2) return 0;
+  if (fin && (v3 - v1) > rhs3) return 1;
+  return 2;
+}
+
+// Top-3 of (value, index) under the order (v, i) < (w, j) iff v < w or
+// (v == w and i < j).  Only the two best keep their index; the third value can
+// never move into the top two when two such lists are merged.
+struct Top3 {
+  float v1, v2, v3;
+  uint32_t i1, i2;
+  __device__ __forceinline__ void init() {
+    v1 = v2 = v3 = __int_as_float(0x7f800000);
+    i1 = i2 = 0xffffffffu;
+  }
+  __device__ __forceinline__ void insert(float v, uint32_t i) {
+    if (v < v1 || (v == v1 && i < i1)) {
+      v3 = v2; v2 = v1; i2 = i1; v1 = v; i1 = i;
+    } else if (v < v2 || (v == v2 && i < i2)) {
+      v3 = v2; v2 = v; i2 = i;
+    } else if (v < v3) {
+      v3 = v;
+    }
+  }
+  __device__ __forceinline__ void merge(const Top3& o) {
+    insert(o.v1, o.i1);
+    insert(o.v2, o.i2);
+    if (o.v3 < v3) v3 = o.v3;
+  }
+  __device__ __forceinline__ void shfl_merge_xor(int mask, unsigned members = 0xffffffffu) {
+    Top3 o;
+    o.v1 = __shfl_xor_sync(members, v1, mask);
+    o.v2 = __shfl_xor_sync(members, v2, mask);
+    o.v3 = __shfl_xor_sync(members, v3, mask);
+    o.i1 = __shfl_xor_sync(members, i1, mask);
+    o.i2 = __shfl_xor_sync(members, i2, mask);
+    merge(o);
+  }
+};
+
+// Refinement queue entry: row index and class/candidates.
+struct RefineEntry {
+  uint32_t row;
+  uint32_t cls;
+  uint32_t c1;
+  uint32_t c2;
+};
+
+// Queue a row for refinement with a warp-aggregated atomic.
+__device__ __forceinline__ void queue_refine(DevState* st, RefineEntry* q, bool want,
+                                             const RefineEntry& e) {
+  const unsigned m = __ballot_sync(__activemask(), want);
+  if (!want) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(&st->flag_count, (uint32_t)__popc(m));
+  base = __shfl_sync(m, base, leader);
+  const uint32_t pos = base + __popc(m & ((1u << lane) - 1u));
+  q[pos] = e;
+}
+
+// Reference CPU distance, bit-exact: float, j ascending, no contraction.
+__device__ __forceinline__ float cpu_dist(const float* __restrict__ x, const float* __restrict__ c,
+                                          uint32_t d) {
+  float s = 0.0f;
+  for (uint32_t j = 0; j < d; ++j) {
+    const float t = __fsub_rn(x[j], c[j]);
+    s = __fadd_rn(s, __fmul_rn(t, t));
+  }
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Bounded waits (mbarrier) and tcgen05 / TMA wrappers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the phase with the given parity to complete, at most `limit_ns`
+// nanoseconds.  Returns false on timeout (or when *abort is raised by a peer).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  volatile int* abort, uint64_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  uint32_t spins = 0;
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((++spins & 63u) == 0) {
+      if (*abort) return false;
+      if (globaltimer_ns() - t0 > limit_ns) return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// 2-D tiled TMA load into shared memory, completing on an mbarrier.
+__device__ __forceinline__ void tma_load_2d(void* smem_dst, const void* tmap, int32_t x, int32_t y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(smem_dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_prefetch_desc(const void* tmap) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(tmap) : "memory");
+}
+
+// tcgen05: TMEM allocation (one warp), MMA (one thread), commit, loads.
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// D(tmem) (+)= A(smem desc) * B(smem desc)^T, kind::f16 (BF16 inputs, FP32 accumulate).
+__device__ __forceinline__ void tc_mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                            uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Arrive on an mbarrier when all previously issued MMAs of this thread complete.
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// 32 lanes x 32 bit, 32 consecutive columns per thread.
+__device__ __forceinline__ void tmem_ld_32x32b_x32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor for a K-major operand in the 128-byte swizzle
+// layout: 8-row groups of 128-byte rows, groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  uint64_t desc = 0;
+  desc |= (uint64_t)((saddr & 0x3FFFFu) >> 4);          // start address
+  desc |= (uint64_t)(16u >> 4) << 16;                    // leading byte offset (unused for SW128 K-major)
+  desc |= (uint64_t)(1024u >> 4) << 32;                  // stride byte offset: 8 rows x 128 B
+  desc |= (uint64_t)1 << 46;                             // descriptor version (tcgen05)
+  desc |= (uint64_t)2 << 61;                             // layout: 128-byte swizzle
+  return desc;
+}
+
+// Instruction descriptor, kind::f16: BF16 A/B, FP32 D, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+// ---------------------------------------------------------------------------
+// Launch helpers implemented in the .cu files.
+// ---------------------------------------------------------------------------
+struct Scratch;  // per-call scratch owned by a handle or a stateless call
+
+}  // namespace km

@@ -1,0 +1,121 @@
+// Lloyd engine: device buffers of one (n, d, k) problem and the launchers of
+// the per-iteration kernel sequence.
+#pragma once
+
+#include <cuda.h>
+#include "km_internal.cuh"
+
+namespace km {
+
+// ---- kernels (km_lloyd_kernels.cu) ----
+__global__ void prep_points_kernel(const float* X, uint64_t n, uint32_t d, uint32_t dp, float* xn2,
+                                   double* xn2d, __nv_bfloat16* Xb, __nv_bfloat16* Xlo,
+                                   DevState* st);
+__global__ void reduce_f64_partial_kernel(const double* v, uint64_t n, double* part);
+__global__ void reduce_f64_final_kernel(const double* part, int np, double* out);
+__global__ void prep_centroids_kernel(const float* C, uint32_t k, uint32_t kp, uint32_t d,
+                                      uint32_t dp, float* cn2, __nv_bfloat16* Cb,
+                                      __nv_bfloat16* Clo, DevState* st);
+__global__ void assign_f32_kernel(const float* X, const float* C, const float* cn2,
+                                  const float* xn2, uint64_t n, uint32_t d, uint32_t k,
+                                  TieBound tb, DevState* st, uint32_t* labels, float* mindist,
+                                  RefineEntry* queue, float* Dout);
+__global__ void refine_kernel(const float* X, const float* C, uint32_t d, uint32_t k, DevState* st,
+                              const RefineEntry* queue, uint32_t* labels, float* mindist);
+__global__ void seg_hist_kernel(const uint32_t* labels, uint64_t n, uint32_t k, uint32_t seg,
+                                uint32_t nseg, uint32_t* seghist, DevState* st);
+__global__ void seg_scan_kernel(uint32_t* seghist, uint32_t k, uint32_t nseg, uint32_t* counts,
+                                DevState* st);
+__global__ void cluster_scan_kernel(const uint32_t* counts, uint32_t k, uint32_t* cstart,
+                                    DevState* st);
+__global__ void seg_scatter_kernel(const uint32_t* labels, uint64_t n, uint32_t k, uint32_t seg,
+                                   uint32_t nseg, const uint32_t* seghist, const uint32_t* cstart,
+                                   uint32_t* perm, DevState* st);
+__global__ void update_sums_kernel(const float* X, const uint32_t* perm, const uint32_t* cstart,
+                                   uint32_t d, uint32_t k, const float* C, float* Cn, float* dsq,
+                                   double* objpart, DevState* st);
+__global__ void finalize_kernel(const float* Cn, float* C, const float* dsq, const double* objpart,
+                                uint32_t d, uint32_t dp, uint32_t k, float tol, float* cn2,
+                                __nv_bfloat16* Cb, __nv_bfloat16* Clo, double* shift_c,
+                                double* obj_c, DevState* st);
+__global__ void control_kernel(const float* cn2, const double* shift_c, const double* obj_c,
+                               uint32_t k, LoopConsts lc, DevState* st);
+
+// ---- tensor-core distance stage (km_tc.cu) ----
+struct TcPlan {
+  bool ok = false;
+  uint32_t KB = 0;       // K blocks of 64 columns
+  uint32_t stages = 0;   // A pipeline depth (K-block units)
+  uint32_t nalloc = 0;   // TMEM columns per accumulator buffer
+  size_t smem = 0;       // dynamic shared memory bytes
+  int grid = 0;
+};
+TcPlan plan_tc(uint32_t dp, uint32_t kp, bool x3, uint64_t n, int num_sms);
+km_status encode_tmap_bf16(CUtensorMap* tm, const void* base, uint64_t inner, uint64_t outer,
+                           uint32_t box_inner, uint32_t box_outer);
+km_status tc_set_attributes(const TcPlan& pl, bool x3);
+km_status launch_assign_tc(const TcPlan& pl, bool x3, const CUtensorMap& tmA,
+                           const CUtensorMap& tmAlo, const CUtensorMap& tmB,
+                           const CUtensorMap& tmBlo, const float* cn2, const float* xn2,
+                           uint64_t n, uint32_t k, uint32_t kp, TieBound tb, DevState* st,
+                           uint32_t* labels, float* mindist, RefineEntry* queue, float* Dout,
+                           cudaStream_t s);
+
+// ---- engine ----
+struct LloydEngine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int num_sms = 0;
+  uint64_t n = 0;
+  uint32_t d = 0, k = 0, dp = 0, kp = 0;
+  int precision = KM_PREC_FP32;
+
+  const float* X = nullptr;   // points (owned copy or borrowed)
+  float* X_owned = nullptr;
+  float* xn2 = nullptr;
+  double* xn2d = nullptr;
+  __nv_bfloat16* Xb = nullptr;
+  __nv_bfloat16* Xlo = nullptr;
+  float* C = nullptr;
+  float* Cn = nullptr;
+  float* cn2 = nullptr;
+  float* dsq = nullptr;
+  double* objpart = nullptr;
+  double* shift_c = nullptr;
+  double* obj_c = nullptr;
+  __nv_bfloat16* Cb = nullptr;
+  __nv_bfloat16* Clo = nullptr;
+  uint32_t* labels = nullptr;
+  float* mindist = nullptr;
+  RefineEntry* queue = nullptr;
+  uint32_t* seghist = nullptr;
+  uint32_t* counts = nullptr;
+  uint32_t* cstart = nullptr;
+  uint32_t* perm = nullptr;
+  double* red_part = nullptr;
+  DevState* st = nullptr;
+  DevState* h_st = nullptr;   // pinned mirror
+  uint32_t seg = 1024, nseg = 0;
+  int sort_wpb = 8;
+  size_t sort_smem = 0;
+  TieBound tb{};
+  TcPlan tc{};
+  CUtensorMap tmA{}, tmAlo{}, tmB{}, tmBlo{};
+  bool data_ready = false;
+
+  ~LloydEngine();
+  km_status init(uint64_t n, uint32_t d, uint32_t k, int precision, int device, void* stream,
+                 bool need_update);
+  km_status set_points(const float* Xsrc, bool on_device, bool copy);
+  km_status set_centroids_dev(const float* Csrc_dev);   // C <- src, prep norms/bf16, cmax
+  km_status reset_state();
+  km_status enqueue_assign(float* Dout);
+  km_status enqueue_sort(const uint32_t* lab);
+  km_status enqueue_update_step(float tol);
+  km_status enqueue_iteration(const LoopConsts& lc);
+  km_status read_state();
+  km_status check_device_error();
+};
+
+}  // namespace km

@@ -1,0 +1,212 @@
+"""ctypes binding of libkm_sm103 (include/km.h) for tests and benchmarks.
+
+The library is the product; this module only marshals arguments.  It raises
+if the shared library has not been built: there is no Python or CPU fallback.
+Device buffers are passed as torch CUDA tensors (data_ptr()).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libkm_sm103.so"
+
+KM_OK, KM_ERR_ARG, KM_ERR_ALLOC, KM_ERR_CUDA, KM_ERR_TIMEOUT, KM_ERR_UNSUPPORTED, KM_ERR_NO_DEVICE, KM_ERR_STATE = range(8)
+INIT_SAMPLE, INIT_ROUND_ROBIN, INIT_GIVEN = 0, 1, 2
+PREC = {"fp32": 0, "bf16": 1, "bf16x3": 2}
+CONV = {"shift": 0, "score": 1, "none": 2}
+KERNEL = {"linear": 0, "polynomial": 1, "sigmoid": 2, "gaussian": 3}
+
+
+class KmError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: {_lib().km_status_str(status).decode()} (status {status})")
+        self.status = status
+
+
+class LloydParams(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("d", C.c_uint32), ("k", C.c_uint32), ("tol", C.c_float),
+                ("seed", C.c_int32), ("maxiter", C.c_uint64), ("init", C.c_int32),
+                ("precision", C.c_int32), ("conv", C.c_int32), ("device", C.c_int32),
+                ("stream", C.c_void_p)]
+
+
+class Result(C.Structure):
+    _fields_ = [("converged_iter", C.c_uint64), ("iterations", C.c_uint64), ("converged", C.c_int32),
+                ("reserved0", C.c_int32), ("objective", C.c_double), ("score", C.c_double),
+                ("max_shift", C.c_double), ("refined_rows", C.c_uint64),
+                ("full_rescore_rows", C.c_uint64), ("fit_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved0"}
+
+
+class KkmParams(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("d", C.c_uint32), ("k", C.c_uint32), ("tol", C.c_float),
+                ("maxiter", C.c_uint64), ("kernel_fn", C.c_int32), ("gamma", C.c_float),
+                ("coef", C.c_float), ("sigma", C.c_float), ("degree", C.c_int32),
+                ("precision", C.c_int32), ("k_bf16", C.c_int32), ("check_converged", C.c_int32),
+                ("device", C.c_int32), ("stream", C.c_void_p)]
+
+
+_LIB = None
+
+# Exported symbols with their ctypes signatures (restype, argtypes).
+SIGNATURES = {
+    "km_status_str": (C.c_char_p, [C.c_int]),
+    "km_version": (C.c_char_p, []),
+    "km_device_count": (C.c_int, []),
+    "km_lloyd_create": (C.c_int, [C.POINTER(LloydParams), C.POINTER(C.c_void_p)]),
+    "km_lloyd_set_data": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "km_lloyd_fit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Result)]),
+    "km_lloyd_device_results": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "km_lloyd_profile": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]),
+    "km_lloyd_destroy": (None, [C.c_void_p]),
+    "km_assign": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int32,
+                            C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64), C.c_void_p]),
+    "km_distances": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int32,
+                               C.c_void_p, C.c_void_p]),
+    "km_update": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p,
+                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "km_kernel_matrix": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_int32, C.c_float, C.c_float,
+                                   C.c_int32, C.c_float, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
+    "km_kkm_create": (C.c_int, [C.POINTER(KkmParams), C.POINTER(C.c_void_p)]),
+    "km_kkm_set_data": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "km_kkm_fit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Result)]),
+    "km_kkm_destroy": (None, [C.c_void_p]),
+    "km_synth_blobs": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, C.c_double, C.c_double, C.c_int32, C.c_uint64, C.c_int32,
+                                 C.c_void_p, C.c_void_p]),
+}
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is not built (run __graft_entry__.build())")
+        lib = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+    return _LIB
+
+
+def lib():
+    return _lib()
+
+
+def check(status: int, what: str):
+    if status != KM_OK:
+        raise KmError(status, what)
+
+
+def device_count() -> int:
+    return _lib().km_device_count()
+
+
+def _ptr(t) -> int:
+    return 0 if t is None else int(t.data_ptr())
+
+
+def synth_blobs(n, d, blobs, lo, hi, sigma, seed, round_clip=False, sigma_range=None, zipf_s=0.0,
+                nthreads=8, with_blob=False):
+    X = np.empty((n, d), np.float32)
+    b = np.empty(n, np.uint32) if with_blob else None
+    slo, shi = sigma_range if sigma_range else (0.0, 0.0)
+    check(_lib().km_synth_blobs(n, d, blobs, lo, hi, sigma, slo, shi, zipf_s, int(round_clip), seed,
+                                nthreads, X.ctypes.data, b.ctypes.data if b is not None else None),
+          "km_synth_blobs")
+    return (X, b) if with_blob else X
+
+
+class Lloyd:
+    """Handle over km_lloyd_*: the Kmeans(...) / run() / get_score() surface."""
+
+    def __init__(self, n, d, k, tol=1e-4, seed=0, maxiter=300, init="sample", precision="fp32",
+                 conv="shift", device=0, stream=0):
+        self.p = LloydParams(n, d, k, tol, seed, maxiter,
+                             {"sample": INIT_SAMPLE, "round_robin": INIT_ROUND_ROBIN, "given": INIT_GIVEN}[init],
+                             PREC[precision], CONV[conv], device, stream or None)
+        h = C.c_void_p()
+        check(_lib().km_lloyd_create(C.byref(self.p), C.byref(h)), "km_lloyd_create")
+        self.h = h
+
+    def set_data(self, X):
+        if isinstance(X, np.ndarray):
+            X = np.ascontiguousarray(X, dtype=np.float32)
+            check(_lib().km_lloyd_set_data(self.h, X.ctypes.data, 0), "km_lloyd_set_data")
+        else:
+            check(_lib().km_lloyd_set_data(self.h, X.data_ptr(), 1), "km_lloyd_set_data")
+        return self
+
+    def fit(self, C0=None, want_centroids=True):
+        n, k, d = self.p.n, self.p.k, self.p.d
+        labels = np.empty(n, np.uint32)
+        cents = np.empty((k, d), np.float32) if want_centroids else None
+        c0 = None
+        if C0 is not None:
+            c0 = np.ascontiguousarray(C0, dtype=np.float32)
+        r = Result()
+        check(_lib().km_lloyd_fit(self.h, c0.ctypes.data if c0 is not None else None, labels.ctypes.data,
+                                  cents.ctypes.data if cents is not None else None, C.byref(r)),
+              "km_lloyd_fit")
+        return labels, cents, r
+
+    def profile(self, iters):
+        """Mean ms per iteration of the five stages (see km_lloyd_profile)."""
+        out = (C.c_double * 5)()
+        check(_lib().km_lloyd_profile(self.h, iters, out), "km_lloyd_profile")
+        return list(out)
+
+    def close(self):
+        if self.h:
+            _lib().km_lloyd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def assign(X, Cc, precision="fp32", want_mindist=False):
+    """labels (and fast-path min distance) of torch CUDA tensors X (n,d), C (k,d)."""
+    import torch
+    n, d = X.shape
+    k = Cc.shape[0]
+    lab = torch.empty(n, dtype=torch.int32, device=X.device)
+    md = torch.empty(n, dtype=torch.float32, device=X.device) if want_mindist else None
+    ref = C.c_uint64(0)
+    check(_lib().km_assign(_ptr(X), _ptr(Cc), n, d, k, PREC[precision], _ptr(lab), _ptr(md), C.byref(ref),
+                           torch.cuda.current_stream().cuda_stream), "km_assign")
+    return lab, md, ref.value
+
+
+def distances(X, Cc, precision="fp32"):
+    import torch
+    n, d = X.shape
+    k = Cc.shape[0]
+    D = torch.empty((n, k), dtype=torch.float32, device=X.device)
+    check(_lib().km_distances(_ptr(X), _ptr(Cc), n, d, k, PREC[precision], _ptr(D),
+                              torch.cuda.current_stream().cuda_stream), "km_distances")
+    return D
+
+
+def update(X, labels, k):
+    import torch
+    n, d = X.shape
+    Cc = torch.empty((k, d), dtype=torch.float32, device=X.device)
+    cnt = torch.empty(k, dtype=torch.int32, device=X.device)
+    perm = torch.empty(n, dtype=torch.int32, device=X.device)
+    off = torch.empty(k + 1, dtype=torch.int32, device=X.device)
+    check(_lib().km_update(_ptr(X), _ptr(labels), n, d, k, _ptr(Cc), _ptr(cnt), _ptr(perm), _ptr(off),
+                           torch.cuda.current_stream().cuda_stream), "km_update")
+    return Cc, cnt, perm, off
