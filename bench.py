@@ -209,6 +209,7 @@ def ours_arm(args, rank, world):
     value = world * iters / (ms_loop / 1000.0)
     fp32_ips = timing["fp32"]["iters"] / (timing["fp32"]["ms_loop"] / 1000.0)
     agree = float((labels[args.precision] == labels["fp32"]).mean())
+    sizes = np.bincount(labels[args.precision], minlength=K)
 
     # per-stage timing with CUDA events on the launching stream
     with torch.cuda.stream(stream):
@@ -288,6 +289,8 @@ def ours_arm(args, rank, world):
         "refined_rows_per_iter": timing[args.precision]["refined"] / max(1, iters),
         "full_rescore_rows_per_iter": timing[args.precision]["full"] / max(1, iters),
         "objective": timing[args.precision]["objective"],
+        "cluster_sizes": {"min": int(sizes.min()), "max": int(sizes.max()), "mean": float(sizes.mean()),
+                          "empty": int((sizes == 0).sum())},
         "stages_ms": dict(zip(names, stages)),
         "roofline": roof,
         "e2e": e2e,

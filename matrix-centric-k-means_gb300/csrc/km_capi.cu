@@ -114,11 +114,8 @@ km_status sample_init(LloydEngine& e, int seed) {
 km_status round_robin_init(LloydEngine& e) {
   round_robin_labels_kernel<<<(unsigned)((e.n + 255) / 256), 256, 0, e.stream>>>(e.labels, e.n, e.k);
   KM_TRY(e.enqueue_sort(e.labels));
-  const uint64_t pairs = (uint64_t)e.k * e.d;
-  update_sums_kernel<<<(unsigned)((pairs + 127) / 128), 128, 0, e.stream>>>(
-      e.X, e.perm, e.cstart, e.d, e.k, nullptr, e.C, nullptr, nullptr, e.st);
-  KM_CUDA_TRY(cudaGetLastError());
-  return KM_OK;
+  return launch_update_sums(e.X, e.perm, e.cstart, e.d, e.k, nullptr, e.C, nullptr, nullptr, e.st,
+                            e.stream);
 }
 
 }  // namespace
@@ -288,26 +285,15 @@ km_status km_lloyd_profile(km_lloyd* h, uint64_t iters, double* stage_ms) {
   km_status rc = KM_OK;
   for (uint64_t it = 0; it < iters && rc == KM_OK; ++it) {
     cudaEventRecord(ev[0], e.stream);
-    if (e.precision == KM_PREC_FP32) {
-      assign_f32_kernel<<<(unsigned)((e.n + 127) / 128), 256, 0, e.stream>>>(
-          e.X, e.C, e.cn2, e.xn2, e.n, e.d, e.k, e.tb, e.st, e.labels, e.mindist, e.queue, nullptr);
-    } else {
-      rc = launch_assign_tc(e.tc, e.precision == KM_PREC_BF16X3, e.tmA, e.tmAlo, e.tmB, e.tmBlo, e.cn2,
-                            e.xn2, e.n, e.k, e.kp, e.tb, e.st, e.labels, e.mindist, e.queue, nullptr, e.stream);
-    }
+    rc = e.enqueue_distance(nullptr);
     cudaEventRecord(ev[1], e.stream);
-    refine_kernel<<<e.num_sms * 4, 256, 0, e.stream>>>(e.X, e.C, e.d, e.k, e.st, e.queue, e.labels, e.mindist);
+    if (rc == KM_OK) rc = e.enqueue_refine();
     cudaEventRecord(ev[2], e.stream);
     if (rc == KM_OK) rc = e.enqueue_sort(e.labels);
     cudaEventRecord(ev[3], e.stream);
-    const uint64_t pairs = (uint64_t)e.k * e.d;
-    update_sums_kernel<<<(unsigned)((pairs + 127) / 128), 128, 0, e.stream>>>(
-        e.X, e.perm, e.cstart, e.d, e.k, e.C, e.Cn, e.dsq, e.objpart, e.st);
+    if (rc == KM_OK) rc = e.enqueue_update_step(h->p.tol);
     cudaEventRecord(ev[4], e.stream);
-    finalize_kernel<<<(e.k * 32 + 255) / 256, 256, 0, e.stream>>>(e.Cn, e.C, e.dsq, e.objpart, e.d, e.dp, e.k,
-                                                                   h->p.tol, e.cn2, e.Cb, e.Clo, e.shift_c,
-                                                                   e.obj_c, e.st);
-    control_kernel<<<1, 256, 0, e.stream>>>(e.cn2, e.shift_c, e.obj_c, e.k, lc, e.st);
+    if (rc == KM_OK) rc = e.enqueue_finalize(lc);
     cudaEventRecord(ev[5], e.stream);
     if (cudaEventSynchronize(ev[5]) != cudaSuccess) { rc = KM_ERR_CUDA; break; }
     for (int s = 0; s < 5; ++s) {
@@ -353,7 +339,7 @@ km_status km_assign(const float* X_dev, const float* C_dev, uint64_t n, uint32_t
   if (mindist_dev)
     KM_CUDA_TRY(cudaMemcpyAsync(mindist_dev, e.mindist, sizeof(float) * n, cudaMemcpyDeviceToDevice, e.stream));
   KM_TRY(e.check_device_error());
-  if (refined_rows) *refined_rows = e.h_st->flag_count;
+  if (refined_rows) *refined_rows = e.h_st->refined_total;
   return KM_OK;
 }
 
@@ -381,10 +367,8 @@ km_status km_update(const float* X_dev, const uint32_t* labels_dev, uint64_t n, 
   e.X = X_dev;
   KM_TRY(e.enqueue_sort(labels_dev));
   KM_TRY(e.check_device_error());   // labels >= k are rejected before the sums run
-  const uint64_t pairs = (uint64_t)k * d;
-  update_sums_kernel<<<(unsigned)((pairs + 127) / 128), 128, 0, e.stream>>>(
-      X_dev, e.perm, e.cstart, d, k, nullptr, C_dev, nullptr, nullptr, e.st);
-  KM_CUDA_TRY(cudaGetLastError());
+  KM_TRY(launch_update_sums(X_dev, e.perm, e.cstart, d, k, nullptr, C_dev, nullptr, nullptr, e.st,
+                            e.stream));
   if (counts_dev) KM_CUDA_TRY(cudaMemcpyAsync(counts_dev, e.counts, sizeof(uint32_t) * k, cudaMemcpyDeviceToDevice, e.stream));
   if (perm_dev) KM_CUDA_TRY(cudaMemcpyAsync(perm_dev, e.perm, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, e.stream));
   if (offsets_dev) KM_CUDA_TRY(cudaMemcpyAsync(offsets_dev, e.cstart, sizeof(uint32_t) * (k + 1), cudaMemcpyDeviceToDevice, e.stream));

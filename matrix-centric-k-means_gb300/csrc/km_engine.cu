@@ -69,7 +69,8 @@ LloydEngine::~LloydEngine() {
   if (device >= 0) cudaSetDevice(device);
   dfree(X_owned); dfree(xn2); dfree(xn2d); dfree(Xb); dfree(Xlo);
   dfree(C); dfree(Cn); dfree(cn2); dfree(dsq); dfree(objpart); dfree(shift_c); dfree(obj_c);
-  dfree(Cb); dfree(Clo); dfree(labels); dfree(mindist); dfree(queue);
+  dfree(Cb); dfree(Clo); dfree(labels); dfree(mindist); dfree(queue); dfree(qfull); dfree(Ct);
+  dfree(qcnt); dfree(qfcnt);
   dfree(seghist); dfree(counts); dfree(cstart); dfree(perm); dfree(red_part); dfree(st);
   if (h_st) cudaFreeHost(h_st);
   if (own_stream && stream) cudaStreamDestroy(stream);
@@ -119,7 +120,15 @@ km_status LloydEngine::init(uint64_t n_, uint32_t d_, uint32_t k_, int precision
   KM_TRY(dalloc(&cn2, kp));
   KM_TRY(dalloc(&labels, n));
   KM_TRY(dalloc(&mindist, n));
-  KM_TRY(dalloc(&queue, n));
+  {
+    const uint64_t rows = (n + 127) / 128 * 128;     // whole 128-row tiles
+    KM_TRY(dalloc(&queue, rows));
+    KM_TRY(dalloc(&qfull, rows));
+    KM_TRY(dalloc(&qcnt, rows / 32));
+    KM_TRY(dalloc(&qfcnt, rows / 32));
+    rq = RefineQueues{queue, qfull, qcnt, qfcnt, rows / 32};
+  }
+  KM_TRY(dalloc(&Ct, (size_t)k * d));
   KM_TRY(dalloc(&red_part, 256));
   KM_TRY(dalloc(&st, 1));
   KM_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&h_st), sizeof(DevState)));
@@ -143,6 +152,7 @@ km_status LloydEngine::init(uint64_t n_, uint32_t d_, uint32_t k_, int precision
     KM_CUDA_TRY(cudaFuncSetAttribute(seg_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem));
   }
   if (need_update) {
+    KM_TRY(update_sums_prepare());
     KM_TRY(dalloc(&Cn, (size_t)k * d));
     KM_TRY(dalloc(&dsq, (size_t)k * d));
     KM_TRY(dalloc(&objpart, (size_t)k * d));
@@ -166,6 +176,7 @@ km_status LloydEngine::set_points(const float* Xsrc, bool on_device, bool copy) 
   } else {
     X = Xsrc;
   }
+  refine_v4 = (d % 4 == 0) && (reinterpret_cast<uintptr_t>(X) % 16 == 0);
   KM_CUDA_TRY(cudaMemsetAsync(&st->err, 0, sizeof(uint32_t), stream));
   const int blocks = (int)std::min<uint64_t>((n + 7) / 8, (uint64_t)num_sms * 16);
   prep_points_kernel<<<blocks, 256, 0, stream>>>(X, n, d, dp, xn2, xn2d, Xb, Xlo, st);
@@ -206,22 +217,34 @@ km_status LloydEngine::set_centroids_dev(const float* Csrc) {
     KM_CUDA_TRY(cudaMemcpyAsync(C, Csrc, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
   KM_CUDA_TRY(cudaMemsetAsync(&st->cmax, 0, sizeof(float), stream));
   const int blocks = (int)((kp * 32 + 255) / 256);
-  prep_centroids_kernel<<<blocks, 256, 0, stream>>>(C, k, kp, d, dp, cn2, Cb, Clo, st);
+  prep_centroids_kernel<<<blocks, 256, 0, stream>>>(C, k, kp, d, dp, cn2, Cb, Clo, Ct, st);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }
 
-km_status LloydEngine::enqueue_assign(float* Dout) {
+km_status LloydEngine::enqueue_distance(float* Dout) {
   if (precision == KM_PREC_FP32) {
-    const unsigned blocks = (unsigned)((n + 127) / 128);
-    assign_f32_kernel<<<blocks, 256, 0, stream>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
-                                                  queue, Dout);
-    KM_CUDA_TRY(cudaGetLastError());
+    KM_TRY(launch_assign_f32(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist, rq, Dout, stream));
   } else {
     KM_TRY(launch_assign_tc(tc, precision == KM_PREC_BF16X3, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k,
-                            kp, tb, st, labels, mindist, queue, Dout, stream));
+                            kp, tb, st, labels, mindist, rq, Dout, stream));
   }
-  refine_kernel<<<num_sms * 4, 256, 0, stream>>>(X, C, d, k, st, queue, labels, mindist);
+  return KM_OK;
+}
+
+km_status LloydEngine::enqueue_refine() {
+  return launch_refine(refine_v4, num_sms, X, C, Ct, d, k, st, rq, labels, mindist, stream);
+}
+
+km_status LloydEngine::enqueue_assign(float* Dout) {
+  KM_TRY(enqueue_distance(Dout));
+  return enqueue_refine();
+}
+
+km_status LloydEngine::enqueue_finalize(const LoopConsts& lc) {
+  finalize_kernel<<<(k * 32 + 255) / 256, 256, 0, stream>>>(Cn, C, dsq, objpart, d, dp, k, lc.tol, cn2,
+                                                            Cb, Clo, Ct, shift_c, obj_c, st);
+  control_kernel<<<1, 256, 0, stream>>>(cn2, shift_c, obj_c, k, lc, st);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }
@@ -238,22 +261,15 @@ km_status LloydEngine::enqueue_sort(const uint32_t* lab) {
 }
 
 km_status LloydEngine::enqueue_update_step(float tol) {
-  const uint64_t pairs = (uint64_t)k * d;
-  update_sums_kernel<<<(unsigned)((pairs + 127) / 128), 128, 0, stream>>>(X, perm, cstart, d, k, C, Cn,
-                                                                          dsq, objpart, st);
-  finalize_kernel<<<(k * 32 + 255) / 256, 256, 0, stream>>>(Cn, C, dsq, objpart, d, dp, k, tol, cn2,
-                                                            Cb, Clo, shift_c, obj_c, st);
-  KM_CUDA_TRY(cudaGetLastError());
-  return KM_OK;
+  (void)tol;
+  return launch_update_sums(X, perm, cstart, d, k, C, Cn, dsq, objpart, st, stream);
 }
 
 km_status LloydEngine::enqueue_iteration(const LoopConsts& lc) {
   KM_TRY(enqueue_assign(nullptr));
   KM_TRY(enqueue_sort(labels));
   KM_TRY(enqueue_update_step(lc.tol));
-  control_kernel<<<1, 256, 0, stream>>>(cn2, shift_c, obj_c, k, lc, st);
-  KM_CUDA_TRY(cudaGetLastError());
-  return KM_OK;
+  return enqueue_finalize(lc);
 }
 
 km_status LloydEngine::read_state() {

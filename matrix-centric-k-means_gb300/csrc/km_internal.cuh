@@ -41,12 +41,12 @@ struct DevState {
   uint32_t iter;            // iterations executed
   uint32_t converged_iter;  // iteration at which the stop rule fired (0: not yet)
   uint32_t moved;           // some centroid moved more than tol in this iteration
-  uint32_t flag_count;      // rows queued for near-tie refinement in this iteration
+  uint32_t pad2;
   uint32_t err;             // device error bits (KM_DEVERR_*)
   uint32_t err_where;       // first wait that ran out (diagnostics)
-  uint32_t pad0;
-  unsigned long long refined_total;
-  unsigned long long full_total;
+  uint32_t pad3;
+  unsigned long long refined_total;  // rows re-scored (all iterations)
+  unsigned long long full_total;     // of those, against all k centroids
   float cmax;               // max_c ||c|| of the centroids the next assignment uses
   float pad1;
   double objective;         // FP64 objective of the last assignment
@@ -128,10 +128,22 @@ struct Top3 {
       v3 = v;
     }
   }
+  // Branch-free insertion under the (v, i) order (selects only, so that lanes
+  // of a warp never diverge).
+  __device__ __forceinline__ void insert_nb(float v, uint32_t i) {
+    const bool c1 = v < v1 || (v == v1 && i < i1);
+    const bool c2 = v < v2 || (v == v2 && i < i2);
+    const bool c3 = v < v3;
+    v3 = c2 ? v2 : (c3 ? v : v3);
+    v2 = c1 ? v1 : (c2 ? v : v2);
+    i2 = c1 ? i1 : (c2 ? i : i2);
+    v1 = c1 ? v : v1;
+    i1 = c1 ? i : i1;
+  }
   __device__ __forceinline__ void merge(const Top3& o) {
-    insert(o.v1, o.i1);
-    insert(o.v2, o.i2);
-    if (o.v3 < v3) v3 = o.v3;
+    insert_nb(o.v1, o.i1);
+    insert_nb(o.v2, o.i2);
+    v3 = fminf(v3, o.v3);
   }
   __device__ __forceinline__ void shfl_merge_xor(int mask, unsigned members = 0xffffffffu) {
     Top3 o;
@@ -144,26 +156,48 @@ struct Top3 {
   }
 };
 
-// Refinement queue entry: row index and class/candidates.
+// Refinement queue entry: a row whose reference argmin is proven to be one of
+// `cnt` (2..4) candidate centroids.  Rows with more candidates go to the
+// full-rescore queue (row index only).
 struct RefineEntry {
   uint32_t row;
-  uint32_t cls;
-  uint32_t c1;
-  uint32_t c2;
+  uint32_t cnt;
+  uint32_t c[4];
 };
 
-// Queue a row for refinement with a warp-aggregated atomic.
-__device__ __forceinline__ void queue_refine(DevState* st, RefineEntry* q, bool want,
-                                             const RefineEntry& e) {
-  const unsigned m = __ballot_sync(__activemask(), want);
-  if (!want) return;
+// The two refinement queues and their per-segment counts.
+struct RefineQueues {
+  RefineEntry* cand;   // rows with 2..4 candidates
+  uint32_t* full;      // rows re-scored against all k
+  uint32_t* ccnt;      // per 32-row segment: entries in cand
+  uint32_t* fcnt;      // per 32-row segment: entries in full
+  uint64_t nseg;       // segments (rows rounded up to whole 128-row tiles, / 32)
+};
+
+// Refinement queues are segmented by rows: the 32 rows r with r >> 5 == seg own
+// slots [32*seg, 32*seg + 32) and a count cnt[seg].  The full warp that
+// classified those rows writes both, so no global counter (and no atomic
+// round-trip on the distance kernels' critical path) is involved, and the
+// queue order is deterministic.  Must be called by all 32 lanes.
+template <class T>
+__device__ __forceinline__ void seg_push(T* q, uint32_t* cnt, uint64_t seg, bool want, const T& e) {
+  const unsigned m = __ballot_sync(0xffffffffu, want);
   const int lane = threadIdx.x & 31;
-  const int leader = __ffs(m) - 1;
-  uint32_t base = 0;
-  if (lane == leader) base = atomicAdd(&st->flag_count, (uint32_t)__popc(m));
-  base = __shfl_sync(m, base, leader);
-  const uint32_t pos = base + __popc(m & ((1u << lane) - 1u));
-  q[pos] = e;
+  if (want) q[seg * 32 + __popc(m & ((1u << lane) - 1u))] = e;
+  if (lane == 0) cnt[seg] = (uint32_t)__popc(m);
+}
+
+// Candidate threshold for one row: every centroid with fast value v(c) > tau
+// has a reference CPU distance strictly above the row's best (the TieBound
+// argument with E1 <= Emax), so the reference argmin lies in {c : v(c) <= tau}.
+__device__ __forceinline__ float tie_tau(float X2, float v1, float cmax, const TieBound& tb) {
+  const float nx = sqrtf(X2) * 1.0000005f;
+  const float T = X2 * 1.0000003f;
+  const float Em = tb.A * nx * cmax + tb.B * cmax * cmax;
+  const float s = fmaxf(0.0f, 2.0f * T + v1 + 2.0f * Em);
+  const float sg = tb.safety * tb.g;
+  float tau = (v1 + tb.safety * (2.0f * Em + tb.g * s) + 1e-30f) / (1.0f - sg);
+  return fmaxf(tau, v1);
 }
 
 // Reference CPU distance, bit-exact: float, j ascending, no contraction.

@@ -15,13 +15,14 @@ __global__ void reduce_f64_partial_kernel(const double* v, uint64_t n, double* p
 __global__ void reduce_f64_final_kernel(const double* part, int np, double* out);
 __global__ void prep_centroids_kernel(const float* C, uint32_t k, uint32_t kp, uint32_t d,
                                       uint32_t dp, float* cn2, __nv_bfloat16* Cb,
-                                      __nv_bfloat16* Clo, DevState* st);
-__global__ void assign_f32_kernel(const float* X, const float* C, const float* cn2,
-                                  const float* xn2, uint64_t n, uint32_t d, uint32_t k,
-                                  TieBound tb, DevState* st, uint32_t* labels, float* mindist,
-                                  RefineEntry* queue, float* Dout);
-__global__ void refine_kernel(const float* X, const float* C, uint32_t d, uint32_t k, DevState* st,
-                              const RefineEntry* queue, uint32_t* labels, float* mindist);
+                                      __nv_bfloat16* Clo, float* Ct, DevState* st);
+km_status launch_assign_f32(const float* X, const float* C, const float* cn2, const float* xn2,
+                            uint64_t n, uint32_t d, uint32_t k, TieBound tb, DevState* st,
+                            uint32_t* labels, float* mindist, const RefineQueues& rq,
+                            float* Dout, cudaStream_t s);
+km_status launch_refine(bool v4, int num_sms, const float* X, const float* C, const float* Ct,
+                        uint32_t d, uint32_t k, DevState* st, const RefineQueues& rq,
+                        uint32_t* labels, float* mindist, cudaStream_t s);
 __global__ void seg_hist_kernel(const uint32_t* labels, uint64_t n, uint32_t k, uint32_t seg,
                                 uint32_t nseg, uint32_t* seghist, DevState* st);
 __global__ void seg_scan_kernel(uint32_t* seghist, uint32_t k, uint32_t nseg, uint32_t* counts,
@@ -31,13 +32,10 @@ __global__ void cluster_scan_kernel(const uint32_t* counts, uint32_t k, uint32_t
 __global__ void seg_scatter_kernel(const uint32_t* labels, uint64_t n, uint32_t k, uint32_t seg,
                                    uint32_t nseg, const uint32_t* seghist, const uint32_t* cstart,
                                    uint32_t* perm, DevState* st);
-__global__ void update_sums_kernel(const float* X, const uint32_t* perm, const uint32_t* cstart,
-                                   uint32_t d, uint32_t k, const float* C, float* Cn, float* dsq,
-                                   double* objpart, DevState* st);
 __global__ void finalize_kernel(const float* Cn, float* C, const float* dsq, const double* objpart,
                                 uint32_t d, uint32_t dp, uint32_t k, float tol, float* cn2,
-                                __nv_bfloat16* Cb, __nv_bfloat16* Clo, double* shift_c,
-                                double* obj_c, DevState* st);
+                                __nv_bfloat16* Cb, __nv_bfloat16* Clo, float* Ct,
+                                double* shift_c, double* obj_c, DevState* st);
 __global__ void control_kernel(const float* cn2, const double* shift_c, const double* obj_c,
                                uint32_t k, LoopConsts lc, DevState* st);
 
@@ -58,8 +56,13 @@ km_status launch_assign_tc(const TcPlan& pl, bool x3, const CUtensorMap& tmA,
                            const CUtensorMap& tmAlo, const CUtensorMap& tmB,
                            const CUtensorMap& tmBlo, const float* cn2, const float* xn2,
                            uint64_t n, uint32_t k, uint32_t kp, TieBound tb, DevState* st,
-                           uint32_t* labels, float* mindist, RefineEntry* queue, float* Dout,
-                           cudaStream_t s);
+                           uint32_t* labels, float* mindist, const RefineQueues& rq,
+                           float* Dout, cudaStream_t s);
+
+km_status update_sums_prepare();
+km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_t* cstart, uint32_t d,
+                             uint32_t k, const float* C, float* Cn, float* dsq, double* objpart,
+                             DevState* st, cudaStream_t s);
 
 // ---- engine ----
 struct LloydEngine {
@@ -89,6 +92,12 @@ struct LloydEngine {
   uint32_t* labels = nullptr;
   float* mindist = nullptr;
   RefineEntry* queue = nullptr;
+  uint32_t* qfull = nullptr;
+  uint32_t* qcnt = nullptr;   // per 32-row segment counts of queue / qfull
+  uint32_t* qfcnt = nullptr;
+  RefineQueues rq{};
+  float* Ct = nullptr;        // centroids transposed (d x k) for the full re-score
+  bool refine_v4 = false;
   uint32_t* seghist = nullptr;
   uint32_t* counts = nullptr;
   uint32_t* cstart = nullptr;
@@ -110,7 +119,10 @@ struct LloydEngine {
   km_status set_points(const float* Xsrc, bool on_device, bool copy);
   km_status set_centroids_dev(const float* Csrc_dev);   // C <- src, prep norms/bf16, cmax
   km_status reset_state();
-  km_status enqueue_assign(float* Dout);
+  km_status enqueue_distance(float* Dout);   // distance + argmin kernel only
+  km_status enqueue_refine();                // exact re-score of the queued rows
+  km_status enqueue_assign(float* Dout);     // both
+  km_status enqueue_finalize(const LoopConsts& lc);
   km_status enqueue_sort(const uint32_t* lab);
   km_status enqueue_update_step(float tol);
   km_status enqueue_iteration(const LoopConsts& lc);

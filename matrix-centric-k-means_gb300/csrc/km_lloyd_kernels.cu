@@ -88,7 +88,8 @@ __global__ void reduce_f64_final_kernel(const double* __restrict__ part, int np,
 __global__ void prep_centroids_kernel(const float* __restrict__ C, uint32_t k, uint32_t kp,
                                       uint32_t d, uint32_t dp, float* __restrict__ cn2,
                                       __nv_bfloat16* __restrict__ Cb,
-                                      __nv_bfloat16* __restrict__ Clo, DevState* st) {
+                                      __nv_bfloat16* __restrict__ Clo, float* __restrict__ Ct,
+                                      DevState* st) {
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= kp) return;
@@ -96,6 +97,7 @@ __global__ void prep_centroids_kernel(const float* __restrict__ C, uint32_t k, u
   double s = 0.0;
   for (uint32_t j = lane; j < dp; j += 32) {
     float v = (c < k && j < d) ? C[(uint64_t)c * d + j] : 0.0f;
+    if (c < k && j < d) Ct[(uint64_t)j * k + c] = v;
     s += (double)v * (double)v;
     if (Cb) {
       __nv_bfloat16 hi = __float2bfloat16_rn(v);
@@ -114,7 +116,8 @@ __global__ void prep_centroids_kernel(const float* __restrict__ C, uint32_t k, u
 // ---------------------------------------------------------------------------
 // (a)+(b) SIMT FP32 distance GEMM with fused top-3 argmin.
 // Tile 128 rows x 128 centroids, 256 threads, 8x8 register micro-tiles,
-// K chunks of 16 staged through shared memory with register double buffering.
+// K chunks of 16 staged through shared memory with register double buffering
+// (16-byte global loads when d % 4 == 0 and the rows are 16-byte aligned).
 // Every CTA walks all centroid tiles for its rows, so the row tile is read from
 // HBM once and re-read from L2.
 // ---------------------------------------------------------------------------
@@ -122,12 +125,13 @@ namespace {
 constexpr int SM_ = 128, SN_ = 128, SK_ = 16, SPAD = 4;
 }
 
+template <bool V4>
 __global__ void __launch_bounds__(256, 1)
 assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
                   const float* __restrict__ cn2, const float* __restrict__ xn2, uint64_t n,
                   uint32_t d, uint32_t k, TieBound tb, DevState* st,
                   uint32_t* __restrict__ labels, float* __restrict__ mindist,
-                  RefineEntry* __restrict__ queue, float* __restrict__ Dout) {
+                  RefineQueues rq, float* __restrict__ Dout) {
   if (st->done) return;
   __shared__ __align__(16) float As[2][SK_][SM_ + SPAD];
   __shared__ __align__(16) float Bs[2][SK_][SN_ + SPAD];
@@ -157,24 +161,53 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
 
     float ra[8], rb[8];
     auto gload = [&](uint32_t kc) {
+      if constexpr (V4) {
 #pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const int idx = e * 256 + tid;
-        const int r = idx >> 4, kk = idx & 15;
-        const uint32_t col = kc + kk;
-        const uint64_t row = m0 + r;
-        ra[e] = (row < n && col < d) ? X[row * d + col] : 0.0f;
-        const uint32_t cc = c0 + r;
-        rb[e] = (cc < k && col < d) ? C[(uint64_t)cc * d + col] : 0.0f;
+        for (int e = 0; e < 2; ++e) {
+          const int idx = e * 256 + tid;
+          const int r = idx >> 2, c4 = idx & 3;
+          const uint32_t col = kc + 4u * (uint32_t)c4;
+          const uint64_t row = m0 + r;
+          const uint32_t cc = c0 + r;
+          float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+          if (row < n && col < d) a = __ldg(reinterpret_cast<const float4*>(X + row * d + col));
+          if (cc < k && col < d) b = __ldg(reinterpret_cast<const float4*>(C + (uint64_t)cc * d + col));
+          ra[4 * e + 0] = a.x; ra[4 * e + 1] = a.y; ra[4 * e + 2] = a.z; ra[4 * e + 3] = a.w;
+          rb[4 * e + 0] = b.x; rb[4 * e + 1] = b.y; rb[4 * e + 2] = b.z; rb[4 * e + 3] = b.w;
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const int idx = e * 256 + tid;
+          const int r = idx >> 4, kk = idx & 15;
+          const uint32_t col = kc + kk;
+          const uint64_t row = m0 + r;
+          ra[e] = (row < n && col < d) ? X[row * d + col] : 0.0f;
+          const uint32_t cc = c0 + r;
+          rb[e] = (cc < k && col < d) ? C[(uint64_t)cc * d + col] : 0.0f;
+        }
       }
     };
     auto sstore = [&](int buf) {
+      if constexpr (V4) {
 #pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const int idx = e * 256 + tid;
-        const int r = idx >> 4, kk = idx & 15;
-        As[buf][kk][r] = ra[e];
-        Bs[buf][kk][r] = rb[e];
+        for (int e = 0; e < 2; ++e) {
+          const int idx = e * 256 + tid;
+          const int r = idx >> 2, c4 = idx & 3;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            As[buf][4 * c4 + q][r] = ra[4 * e + q];
+            Bs[buf][4 * c4 + q][r] = rb[4 * e + q];
+          }
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const int idx = e * 256 + tid;
+          const int r = idx >> 4, kk = idx & 15;
+          As[buf][kk][r] = ra[e];
+          Bs[buf][kk][r] = rb[e];
+        }
       }
     };
     gload(0);
@@ -212,7 +245,7 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
         const uint32_t col = c0 + tx * 8 + j;
         const float v = fmaf(-2.0f, acc[i][j], cns[tx * 8 + j]);
         if (Dout && row < n && col < k) Dout[row * k + col] = v + xn2[row];
-        if (col < k) t.insert(v, col);
+        if (col < k) t.insert_nb(v, col);
       }
       t.shfl_merge_xor(8);
       t.shfl_merge_xor(4);
@@ -240,38 +273,140 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
       labels[row] = i1;
       if (mindist) mindist[row] = bv1[tid] + xn2[row];
     }
-    RefineEntry e{(uint32_t)row, (uint32_t)cls, i1, bi2[tid]};
-    queue_refine(st, queue, valid && cls != 0, e);
+    RefineEntry e{(uint32_t)row, 2u, {i1, bi2[tid], 0u, 0u}};
+    const uint64_t seg = row >> 5;
+    seg_push(rq.cand, rq.ccnt, seg, valid && cls == 1, e);
+    seg_push(rq.full, rq.fcnt, seg, valid && cls == 2, (uint32_t)row);
   }
 }
 
-// Exact refinement of queued rows: one warp per row; the reference's CPU
-// distance (float, j ascending) to the candidates, lowest index on ties.
-__global__ void refine_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
-                              uint32_t k, DevState* st, const RefineEntry* __restrict__ queue,
-                              uint32_t* __restrict__ labels, float* __restrict__ mindist) {
+km_status launch_assign_f32(const float* X, const float* C, const float* cn2, const float* xn2,
+                            uint64_t n, uint32_t d, uint32_t k, TieBound tb, DevState* st,
+                            uint32_t* labels, float* mindist, const RefineQueues& rq,
+                            float* Dout, cudaStream_t s) {
+  const unsigned blocks = (unsigned)((n + SM_ - 1) / SM_);
+  const bool v4 = (d % 4 == 0) && (reinterpret_cast<uintptr_t>(X) % 16 == 0) &&
+                  (reinterpret_cast<uintptr_t>(C) % 16 == 0);
+  if (v4)
+    assign_f32_kernel<true><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
+                                                   rq, Dout);
+  else
+    assign_f32_kernel<false><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
+                                                    rq, Dout);
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
+
+// Reference CPU distance of one row to one centroid with 16-byte loads (d % 4
+// == 0 and 16-byte aligned rows); the operation order is unchanged.
+__device__ __forceinline__ float cpu_dist_v4(const float* __restrict__ x, const float* __restrict__ c,
+                                             uint32_t d) {
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+  const float4* c4 = reinterpret_cast<const float4*>(c);
+  float s = 0.0f;
+  for (uint32_t q = 0; q < d / 4; ++q) {
+    const float4 a = x4[q], b = c4[q];
+    float t = __fsub_rn(a.x, b.x); s = __fadd_rn(s, __fmul_rn(t, t));
+    t = __fsub_rn(a.y, b.y); s = __fadd_rn(s, __fmul_rn(t, t));
+    t = __fsub_rn(a.z, b.z); s = __fadd_rn(s, __fmul_rn(t, t));
+    t = __fsub_rn(a.w, b.w); s = __fadd_rn(s, __fmul_rn(t, t));
+  }
+  return s;
+}
+
+// Exact re-score of rows with 2..4 candidates: four lanes per row, one
+// candidate per lane, the reference's CPU distance (float, j ascending);
+// smallest distance wins, lowest index on ties.  The candidate set provably
+// holds the reference argmin over all k (tie_tau / tie_class).
+template <bool V4>
+__global__ void __launch_bounds__(256)
+refine_cands_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
+                    DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
+                    float* __restrict__ mindist) {
   if (st->done) return;
-  const uint32_t cnt = st->flag_count;
   const int lane = threadIdx.x & 31;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t e = warp; e < cnt; e += nw) {
-    const RefineEntry en = queue[e];
-    const float* x = X + (uint64_t)en.row * d;
-    float bv = f_inf();
-    uint32_t bi = 0xffffffffu;
-    if (en.cls == 1) {
-      if (lane < 2) {
-        const uint32_t c = lane ? en.c2 : en.c1;
-        if (c < k) {
-          const float v = cpu_dist(x, C + (uint64_t)c * d, d);
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint32_t done_rows = 0;
+  for (uint64_t seg = warp; seg < rq.nseg; seg += nw) {
+    const uint32_t cnt = rq.ccnt[seg];
+    done_rows += cnt;
+    for (uint32_t base = 0; base < cnt; base += 8) {
+      const uint32_t e = base + (uint32_t)(lane >> 2);
+      const uint32_t slot = lane & 3;
+      float bv = f_inf();
+      uint32_t bi = 0xffffffffu;
+      uint32_t row = 0;
+      if (e < cnt) {
+        const RefineEntry en = rq.cand[seg * 32 + e];
+        row = en.row;
+        if (slot < en.cnt) {
+          const uint32_t c = en.c[slot];
+          const float* x = X + (uint64_t)row * d;
+          const float* cc = C + (uint64_t)c * d;
+          const float v = V4 ? cpu_dist_v4(x, cc, d) : cpu_dist(x, cc, d);
           if (v < bv) { bv = v; bi = c; }
         }
       }
-    } else {
-      for (uint32_t c = lane; c < k; c += 32) {
-        const float v = cpu_dist(x, C + (uint64_t)c * d, d);
-        if (v < bv) { bv = v; bi = c; }
+#pragma unroll
+      for (int o = 1; o <= 2; o <<= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+      }
+      if (e < cnt && slot == 0) {
+        labels[row] = (bi == 0xffffffffu) ? 0u : bi;
+        if (mindist) mindist[row] = bv;
+      }
+    }
+  }
+  if (lane == 0 && done_rows) atomicAdd(&st->refined_total, (unsigned long long)done_rows);
+}
+
+// Exact re-score against all k centroids: one warp per row, lanes over
+// centroids (eight chains per lane), centroids read from the transposed copy
+// Ct (d x k) so that every load of the warp is one coalesced 128-byte line.
+// Per lane the centroids are visited in ascending order with a strict '<'
+// and the warp reduction keeps the lowest index on ties: the reference's
+// argmin (kmeans.cpp:106-122).
+__global__ void __launch_bounds__(256)
+refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, uint32_t d, uint32_t k,
+                   DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
+                   float* __restrict__ mindist) {
+  if (st->done) return;
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  // Work items: (segment, entry) pairs, one warp each; segments are walked in
+  // warp-strided order and each of their entries handed out in turn.
+  uint32_t done_rows = 0;
+  for (uint64_t seg = warp; seg < rq.nseg; seg += nw) {
+   const uint32_t cnt = rq.fcnt[seg];
+   done_rows += cnt;
+   for (uint32_t e = 0; e < cnt; ++e) {
+    const uint32_t row = rq.full[seg * 32 + e];
+    const float* x = X + (uint64_t)row * d;
+    float bv = f_inf();
+    uint32_t bi = 0xffffffffu;
+    for (uint32_t cb = 0; cb < k; cb += 256) {
+      float s[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) s[t] = 0.0f;
+      for (uint32_t j = 0; j < d; ++j) {
+        const float xj = x[j];
+        const float* ct = Ct + (uint64_t)j * k + cb + lane;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          if (cb + lane + 32 * t < k) {
+            const float tt = __fsub_rn(xj, ct[32 * t]);
+            s[t] = __fadd_rn(s[t], __fmul_rn(tt, tt));
+          }
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const uint32_t c = cb + lane + 32 * t;
+        if (c < k && s[t] < bv) { bv = s[t]; bi = c; }
       }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -280,11 +415,27 @@ __global__ void refine_kernel(const float* __restrict__ X, const float* __restri
       if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
     }
     if (lane == 0) {
-      labels[en.row] = (bi == 0xffffffffu) ? 0u : bi;
-      if (mindist) mindist[en.row] = bv;
-      if (en.cls == 2) atomicAdd(&st->full_total, 1ull);
+      labels[row] = (bi == 0xffffffffu) ? 0u : bi;
+      if (mindist) mindist[row] = bv;
     }
+   }
   }
+  if (lane == 0 && done_rows) {
+    atomicAdd(&st->refined_total, (unsigned long long)done_rows);
+    atomicAdd(&st->full_total, (unsigned long long)done_rows);
+  }
+}
+
+km_status launch_refine(bool v4, int num_sms, const float* X, const float* C, const float* Ct,
+                        uint32_t d, uint32_t k, DevState* st, const RefineQueues& rq,
+                        uint32_t* labels, float* mindist, cudaStream_t s) {
+  if (v4)
+    refine_cands_kernel<true><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
+  else
+    refine_cands_kernel<false><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
+  refine_full_kernel<<<num_sms * 4, 256, 0, s>>>(X, Ct, d, k, st, rq, labels, mindist);
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -395,59 +546,174 @@ __global__ void seg_scatter_kernel(const uint32_t* __restrict__ labels, uint64_t
 }
 
 // ---------------------------------------------------------------------------
-// (c) Exact centroid update V.X: thread per (cluster, column), rows of the
-// cluster in ascending index order (the label-sorted permutation), float sums
-// exactly as the reference's CPU loop.  Also: squared move per element for the
-// shift test, and the FP64 objective of this iteration's assignment against the
-// centroids that produced it (FP32 partials over 64 rows, FP64 above).
+// (c) Exact centroid update V.X.  One warp per (cluster, 32*VEC-column chunk),
+// each lane on VEC adjacent columns: the cluster's rows are visited in
+// ascending index order (the label-sorted permutation) and summed in float
+// exactly as the reference's CPU loop (kmeans.cpp:133-137).  Row segments are
+// gathered with cp.async (16 bytes per lane for VEC = 4, 4 bytes for VEC = 1,
+// zero-filled past d) into a per-warp ring of UPD_STAGES batches of UPD_ROWS
+// rows, so that three batches are in flight while the ordered additions consume
+// the fourth; the permutation indices of a batch come in with one coalesced
+// load and are broadcast by shuffles.  Also: squared move per element for the
+// shift test and the FP64 objective of this iteration's assignment against the
+// centroids that produced it (FP32 partials per batch, FP64 above).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128)
+namespace {
+constexpr int UPD_ROWS = 32, UPD_STAGES = 8;
+
+__device__ __forceinline__ void cp_async_16(void* smem, const void* gmem, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem)), "l"(gmem),
+               "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_4(void* smem, const void* gmem, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(smem)), "l"(gmem),
+               "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+}  // namespace
+
+template <int VEC>
+__global__ void __launch_bounds__(32)
 update_sums_kernel(const float* __restrict__ X, const uint32_t* __restrict__ perm,
                    const uint32_t* __restrict__ cstart, uint32_t d, uint32_t k,
                    const float* __restrict__ C, float* __restrict__ Cn,
                    float* __restrict__ dsq, double* __restrict__ objpart, DevState* st) {
   if (st && st->done) return;
-  const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= (uint64_t)k * d) return;
-  const uint32_t c = (uint32_t)(p / d), j = (uint32_t)(p % d);
+  extern __shared__ __align__(16) float ring[];   // [UPD_STAGES][UPD_ROWS][32 * VEC]
+  constexpr uint32_t W = 32u * VEC;
+  const uint32_t nchunk = (d + W - 1) / W;
+  const uint64_t gw = blockIdx.x;
+  if (gw >= (uint64_t)k * nchunk) return;
+  const int lane = threadIdx.x & 31;
+  const uint32_t c = (uint32_t)(gw / nchunk);
+  const uint32_t j0 = (uint32_t)(gw % nchunk) * W + (uint32_t)lane * VEC;
   const uint32_t s0 = cstart[c], s1 = cstart[c + 1];
-  const float cold = C ? C[p] : 0.0f;
-  float sum = 0.0f, e32 = 0.0f;
-  double e64 = 0.0;
-  constexpr int U = 16;
-  uint32_t s = s0;
-  int chunk = 0;
-  for (; s + U <= s1; s += U) {
-    uint32_t r[U];
-    float v[U];
+  const uint32_t nb = (s1 - s0 + UPD_ROWS - 1) / UPD_ROWS;
+  float cold[VEC], sum[VEC];
+  double e64[VEC];
 #pragma unroll
-    for (int u = 0; u < U; ++u) r[u] = perm[s + u];
-#pragma unroll
-    for (int u = 0; u < U; ++u) v[u] = X[(uint64_t)r[u] * d + j];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      sum = __fadd_rn(sum, v[u]);
-      const float t = v[u] - cold;
-      e32 = fmaf(t, t, e32);
+  for (int q = 0; q < VEC; ++q) {
+    cold[q] = (C && j0 + q < d) ? C[(uint64_t)c * d + j0 + q] : 0.0f;
+    sum[q] = 0.0f;
+    e64[q] = 0.0;
+  }
+  // Permutation index of this lane's row in batch b (loaded one batch ahead of
+  // its use so that the gather issue never waits on it).
+  auto load_perm = [&](uint32_t b) -> uint32_t {
+    const uint32_t i = s0 + b * UPD_ROWS + (uint32_t)lane;
+    return (b < nb && i < s1) ? perm[i] : 0u;
+  };
+  auto issue = [&](uint32_t b, uint32_t rl) {
+    if (b < nb) {
+      const uint32_t base = s0 + b * UPD_ROWS;
+      const uint32_t m = min((uint32_t)UPD_ROWS, s1 - base);
+      float* dst = ring + (size_t)(b % UPD_STAGES) * UPD_ROWS * W + (uint32_t)lane * VEC;
+#pragma unroll 8
+      for (int u = 0; u < UPD_ROWS; ++u) {
+        const uint32_t r = __shfl_sync(0xffffffffu, rl, u);
+        const bool ok = (uint32_t)u < m && j0 < d;
+        const float* src = ok ? X + (uint64_t)r * d + j0 : X;
+        if constexpr (VEC == 4) cp_async_16(dst + (size_t)u * W, src, ok ? 16u : 0u);
+        else cp_async_4(dst + (size_t)u * W, src, ok ? 4u : 0u);
+      }
     }
-    if (++chunk == 4) { e64 += e32; e32 = 0.0f; chunk = 0; }
+    cp_async_commit();
+  };
+  {
+    uint32_t p0[UPD_STAGES - 1];
+#pragma unroll
+    for (int b = 0; b < UPD_STAGES - 1; ++b) p0[b] = load_perm((uint32_t)b);
+#pragma unroll
+    for (int b = 0; b < UPD_STAGES - 1; ++b) issue((uint32_t)b, p0[b]);
   }
-  for (; s < s1; ++s) {
-    const float v = X[(uint64_t)perm[s] * d + j];
-    sum = __fadd_rn(sum, v);
-    const float t = v - cold;
-    e32 = fmaf(t, t, e32);
+  // pq[i] holds the permutation indices of batch b + UPD_STAGES - 1 + i: the
+  // load of a batch's indices is issued UPD_PREFETCH iterations before use.
+  constexpr int UPD_PREFETCH = 8;
+  uint32_t pq[UPD_PREFETCH];
+#pragma unroll
+  for (int i = 0; i < UPD_PREFETCH; ++i) pq[i] = load_perm((uint32_t)(UPD_STAGES - 1 + i));
+  for (uint32_t b = 0; b < nb; ++b) {
+    const uint32_t cur = pq[0];
+#pragma unroll
+    for (int i = 0; i + 1 < UPD_PREFETCH; ++i) pq[i] = pq[i + 1];
+    pq[UPD_PREFETCH - 1] = load_perm(b + UPD_STAGES - 1 + UPD_PREFETCH);
+    issue(b + UPD_STAGES - 1, cur);
+    cp_async_wait<UPD_STAGES - 1>();
+    __syncwarp();
+    const uint32_t m = min((uint32_t)UPD_ROWS, s1 - (s0 + b * UPD_ROWS));
+    const float* src = ring + (size_t)(b % UPD_STAGES) * UPD_ROWS * W + (uint32_t)lane * VEC;
+    float e32[VEC];
+#pragma unroll
+    for (int q = 0; q < VEC; ++q) e32[q] = 0.0f;
+#pragma unroll 8
+    for (int u = 0; u < UPD_ROWS; ++u) {
+      if ((uint32_t)u < m) {
+        float v[VEC];
+        if constexpr (VEC == 4) {
+          const float4 f = *reinterpret_cast<const float4*>(src + (size_t)u * W);
+          v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
+        } else {
+          v[0] = src[(size_t)u * W];
+        }
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) {
+          sum[q] = __fadd_rn(sum[q], v[q]);
+          const float t = v[q] - cold[q];
+          e32[q] = fmaf(t, t, e32[q]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < VEC; ++q) e64[q] += e32[q];
+    __syncwarp();
   }
-  e64 += e32;
+  cp_async_wait<0>();
   const uint32_t cnt = s1 - s0;
   const float scale = __double2float_rn(1.0 / (double)(cnt > 1 ? cnt : 1));
-  const float cn = __fmul_rn(sum, scale);
-  Cn[p] = cn;
-  if (dsq) {
-    const float t = __fsub_rn(cn, cold);
-    dsq[p] = __fmul_rn(t, t);
+#pragma unroll
+  for (int q = 0; q < VEC; ++q) {
+    if (j0 + q >= d) break;
+    const uint64_t p = (uint64_t)c * d + j0 + q;
+    const float cn = __fmul_rn(sum[q], scale);
+    Cn[p] = cn;
+    if (dsq) {
+      const float t = __fsub_rn(cn, cold[q]);
+      dsq[p] = __fmul_rn(t, t);
+    }
+    if (objpart) objpart[p] = e64[q];
   }
-  if (objpart) objpart[p] = e64;
+}
+
+// Opt-in shared memory for the VEC = 4 ring; called before any capture.
+km_status update_sums_prepare() {
+  KM_CUDA_TRY(cudaFuncSetAttribute(update_sums_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   UPD_STAGES * UPD_ROWS * 128 * (int)sizeof(float)));
+  return KM_OK;
+}
+
+// One lane per column (32 columns per warp) exposes the most independent
+// (cluster, column) chains: the largest cluster is spread over d/32 warps, each
+// with UPD_STAGES*UPD_ROWS rows in flight.  The 4-column variant is used only
+// when the chains already outnumber the GPU many times over.
+km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_t* cstart, uint32_t d,
+                             uint32_t k, const float* C, float* Cn, float* dsq, double* objpart,
+                             DevState* st, cudaStream_t s) {
+  const bool v4 = (d % 4 == 0) && (reinterpret_cast<uintptr_t>(X) % 16 == 0) &&
+                  (uint64_t)k * ((d + 127) / 128) >= 4096;
+  const uint32_t W = v4 ? 128u : 32u;
+  const uint64_t warps = (uint64_t)k * ((d + W - 1) / W);
+  const size_t smem = (size_t)UPD_STAGES * UPD_ROWS * W * sizeof(float);
+  if (v4) {
+    update_sums_kernel<4><<<(unsigned)warps, 32, smem, s>>>(X, perm, cstart, d, k, C, Cn, dsq, objpart, st);
+  } else {
+    update_sums_kernel<1><<<(unsigned)warps, 32, smem, s>>>(X, perm, cstart, d, k, C, Cn, dsq, objpart, st);
+  }
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
 }
 
 // One warp per cluster: reference shift test (float sum over j ascending, then
@@ -457,8 +723,9 @@ __global__ void finalize_kernel(const float* __restrict__ Cn, float* __restrict_
                                 const float* __restrict__ dsq, const double* __restrict__ objpart,
                                 uint32_t d, uint32_t dp, uint32_t k, float tol,
                                 float* __restrict__ cn2, __nv_bfloat16* __restrict__ Cb,
-                                __nv_bfloat16* __restrict__ Clo, double* __restrict__ shift_c,
-                                double* __restrict__ obj_c, DevState* st) {
+                                __nv_bfloat16* __restrict__ Clo, float* __restrict__ Ct,
+                                double* __restrict__ shift_c, double* __restrict__ obj_c,
+                                DevState* st) {
   if (st->done) return;
   const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -472,6 +739,7 @@ __global__ void finalize_kernel(const float* __restrict__ Cn, float* __restrict_
       const double t = (double)v - (double)C[base + j];
       mv += t * t;
       ob += objpart[base + j];
+      Ct[(uint64_t)j * k + c] = v;
     }
     if (Cb) {
       const __nv_bfloat16 hi = __float2bfloat16_rn(v);
@@ -532,8 +800,6 @@ __global__ void control_kernel(const float* __restrict__ cn2, const double* __re
     st->cmax = s_cm[0] * 1.000001f;
     const double score = s_obj[0] - st->sum_x2;
     st->score = score;
-    st->refined_total += st->flag_count;
-    st->flag_count = 0;
     bool stop = false;
     if (lc.conv == KM_CONV_SHIFT) {
       if (it > 1 && st->moved == 0u) { st->converged_iter = it; stop = true; }

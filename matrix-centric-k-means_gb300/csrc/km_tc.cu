@@ -8,11 +8,18 @@
 // accumulator buffers (kp columns each) let the epilogue of tile t overlap the
 // MMAs of tile t+1.
 //
-//   warp 0      TMA producer (one elected lane)
-//   warp 1      MMA issuer (one elected lane)
-//   warp 2      TMEM allocator
-//   warps 4-11  epilogue: warp w reads TMEM lanes 32*(w%4).., half the column
-//               chunks each; v = ||c||^2 - 2 acc, top-3 per row, near-tie class.
+//   warp 0       TMA producer (one elected lane)
+//   warp 1       MMA issuer (one elected lane)
+//   warp 2       TMEM allocator
+//   warps 4-19   epilogue, four warps per TMEM lane quadrant (warp w reads
+//                lanes 32*(w%4)..+31), each on a quarter of the column chunks:
+//                pass 1  v = ||c||^2 - 2 acc kept in registers, row minimum v1;
+//                        the TMEM buffer is released right after the loads;
+//                pass 2  candidates {c : v(c) <= tau(v1)} (tie_tau); one
+//                        candidate: the label is proven; 2..4: queued for the
+//                        exact re-score of those; more: full re-score.
+//                The four warps of a quadrant combine through shared memory
+//                with bounded mbarrier hand-offs.
 //
 // Every mbarrier wait is bounded (2 s); on timeout the CTA raises an abort
 // flag, records KM_DEVERR_TIMEOUT, waits (bounded) for its own copies and MMAs
@@ -32,7 +39,8 @@ namespace km {
 
 namespace {
 
-constexpr int TC_THREADS = 384;
+constexpr int TC_EPI_WARPS = 16;
+constexpr int TC_THREADS = 32 * (4 + TC_EPI_WARPS);
 constexpr int TC_M = 128;
 constexpr uint64_t WAIT_NS = 2000000000ull;
 constexpr uint32_t A_UNIT = TC_M * 128;  // bytes of one 128-row x 64-col BF16 K-block
@@ -44,12 +52,13 @@ struct TcSmem {
   uint64_t tfull[2];
   uint64_t tempty[2];
   uint64_t tdone;
-  uint64_t xfull[4];
-  uint64_t xempty[4];
+  uint64_t x1[4];     // per quadrant: partial minima written
+  uint64_t x2[4];     // per quadrant: partial candidate lists written
   uint32_t tmem_base;
   int abort;
-  float xv1[TC_M], xv2[TC_M], xv3[TC_M];
-  uint32_t xi1[TC_M], xi2[TC_M];
+  float xmin[4][TC_M];
+  uint32_t xcnt[4][TC_M];
+  uint32_t xcand[4][TC_M][4];
 };
 
 template <bool X3>
@@ -59,7 +68,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
                  const float* __restrict__ cn2, const float* __restrict__ xn2, uint64_t n,
                  uint32_t k, uint32_t kp, uint32_t KB, uint32_t S, uint32_t nalloc, TieBound tb,
                  DevState* st, uint32_t* __restrict__ labels, float* __restrict__ mindist,
-                 RefineEntry* __restrict__ queue, float* __restrict__ Dout) {
+                 RefineQueues rq, float* __restrict__ Dout) {
   if (st->done) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -69,7 +78,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   uint8_t* sA = smem + b_bytes * (X3 ? 2u : 1u);
   const uint32_t unit_bytes = A_UNIT * (X3 ? 2u : 1u);
   float* cns = reinterpret_cast<float*>(sA + (size_t)S * unit_bytes);
-  TcSmem* ts = reinterpret_cast<TcSmem*>(cns + ((kp + 3) & ~3u));
+  TcSmem* ts = reinterpret_cast<TcSmem*>(cns + ((kp + 31) & ~31u));
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t ntiles = (n + TC_M - 1) / TC_M;
@@ -78,13 +87,15 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   if (threadIdx.x == 0) {
     for (uint32_t s = 0; s < S; ++s) { mbar_init(&ts->full[s], 1); mbar_init(&ts->empty[s], 1); }
     mbar_init(&ts->bfull, 1);
-    for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], 8); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], TC_EPI_WARPS); }
     mbar_init(&ts->tdone, 1);
-    for (int q = 0; q < 4; ++q) { mbar_init(&ts->xfull[q], 32); mbar_init(&ts->xempty[q], 32); }
+    for (int q = 0; q < 4; ++q) { mbar_init(&ts->x1[q], 128); mbar_init(&ts->x2[q], 128); }
     ts->abort = 0;
     mbar_fence_init();
   }
-  for (uint32_t c = threadIdx.x; c < kp; c += blockDim.x) cns[c] = (c < k) ? cn2[c] : __int_as_float(0x7f800000);
+  const uint32_t kp32 = (kp + 31) & ~31u;
+  for (uint32_t c = threadIdx.x; c < kp32; c += blockDim.x)
+    cns[c] = (c < k) ? cn2[c] : __int_as_float(0x7f800000);
   if (warp == 2) tmem_alloc(&ts->tmem_base, 2u * nalloc);
   tc_fence_before();
   __syncthreads();
@@ -175,64 +186,109 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       }
     }
   } else if (warp >= 4) {
-    const int q = warp & 3, h = (warp - 4) >> 2;
-    const uint32_t nch = (kp + 31) / 32;
+    const int q = warp & 3, sub = (warp - 4) >> 2;
+    const uint32_t nch = (kp + 31) / 32;            // <= 8, so <= 2 chunks per warp
+    const uint32_t r = (uint32_t)q * 32u + (uint32_t)lane;
     uint64_t t = 0;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
-      const uint32_t buf = (uint32_t)(t & 1u), use = (uint32_t)(t >> 1);
-      const bool ok = mbar_wait_bounded(&ts->tfull[buf], use & 1u, abort_flag, WAIT_NS);
-      if (!__all_sync(0xffffffffu, ok)) { if (lane == 0) fail(5); break; }
+      const uint32_t buf = (uint32_t)(t & 1u), use = (uint32_t)(t >> 1), xp = (uint32_t)(t & 1u);
+      const bool okw = mbar_wait_bounded(&ts->tfull[buf], use & 1u, abort_flag, WAIT_NS);
+      if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(5); break; }
       tc_fence_after();
-      const uint32_t r = (uint32_t)q * 32u + (uint32_t)lane;
       const uint64_t row = tile * TC_M + r;
       const float x2 = (row < n) ? xn2[row] : 0.0f;
-      Top3 best;
-      best.init();
-      for (uint32_t ch = (uint32_t)h; ch < nch; ch += 2) {
-        uint32_t v[32];
-        tmem_ld_32x32b_x32(tmem_base + (((uint32_t)q * 32u) << 16) + buf * nalloc + ch * 32u, v);
-        tmem_ld_wait();
+      // ---- pass 1: values into registers, row minimum ----
+      float v[64];
+      float m0 = __int_as_float(0x7f800000), m1 = m0, m2 = m0, m3 = m0;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const uint32_t col = ch * 32u + (uint32_t)j;
-          if (col < k) {
-            const float dv = fmaf(-2.0f, __uint_as_float(v[j]), cns[col]);
-            best.insert(dv, col);
-            if (Dout && row < n) Dout[row * k + col] = dv + x2;
+      for (int c2 = 0; c2 < 2; ++c2) {
+        const uint32_t ch = (uint32_t)sub + 4u * (uint32_t)c2;
+        if (ch < nch) {
+          uint32_t acc[32];
+          tmem_ld_32x32b_x32(tmem_base + (((uint32_t)q * 32u) << 16) + buf * nalloc + ch * 32u, acc);
+          tmem_ld_wait();
+          const float4* cn4 = reinterpret_cast<const float4*>(cns + ch * 32u);
+#pragma unroll
+          for (int j4 = 0; j4 < 8; ++j4) {
+            const float4 cc = cn4[j4];
+            const float a = fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 0]), cc.x);
+            const float b = fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 1]), cc.y);
+            const float c = fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 2]), cc.z);
+            const float e = fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 3]), cc.w);
+            v[c2 * 32 + 4 * j4 + 0] = a; v[c2 * 32 + 4 * j4 + 1] = b;
+            v[c2 * 32 + 4 * j4 + 2] = c; v[c2 * 32 + 4 * j4 + 3] = e;
+            m0 = fminf(m0, a); m1 = fminf(m1, b); m2 = fminf(m2, c); m3 = fminf(m3, e);
           }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[c2 * 32 + j] = __int_as_float(0x7f800000);
         }
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&ts->tempty[buf]);
-      // The two warps of a lane quadrant merge through shared memory, handing
-      // the buffer over with bounded mbarrier waits (never a bare bar.sync, so
-      // a warp that stopped on a timeout cannot strand its partner).
-      const uint32_t xp = (uint32_t)(t & 1u);
-      if (h == 1) {
-        const bool okx = mbar_wait_bounded(&ts->xempty[q], xp ^ 1u, abort_flag, WAIT_NS);
-        if (!__all_sync(0xffffffffu, okx)) { if (lane == 0) fail(6); break; }
-        ts->xv1[r] = best.v1; ts->xv2[r] = best.v2; ts->xv3[r] = best.v3;
-        ts->xi1[r] = best.i1; ts->xi2[r] = best.i2;
-        mbar_arrive(&ts->xfull[q]);
-      } else {
-        const bool okx = mbar_wait_bounded(&ts->xfull[q], xp, abort_flag, WAIT_NS);
-        if (!__all_sync(0xffffffffu, okx)) { if (lane == 0) fail(7); break; }
-        Top3 o;
-        o.v1 = ts->xv1[r]; o.v2 = ts->xv2[r]; o.v3 = ts->xv3[r]; o.i1 = ts->xi1[r]; o.i2 = ts->xi2[r];
-        mbar_arrive(&ts->xempty[q]);
-        best.merge(o);
-        const bool valid = row < n;
-        const uint32_t i1 = best.i1 == 0xffffffffu ? 0u : best.i1;
-        int cls = 0;
-        if (valid) {
-          const float cn1 = sqrtf(fmaxf(cns[i1], 0.0f));
-          cls = tie_class(x2, best.v1, best.v2, best.v3, cn1, cmax, tb);
-          labels[row] = i1;
-          if (mindist) mindist[row] = best.v1 + x2;
+      if (lane == 0) mbar_arrive(&ts->tempty[buf]);     // accumulator buffer free
+      if (Dout && row < n) {
+#pragma unroll
+        for (int c2 = 0; c2 < 2; ++c2) {
+          const uint32_t ch = (uint32_t)sub + 4u * (uint32_t)c2;
+          if (ch < nch)
+            for (int j = 0; j < 32; ++j)
+              if (ch * 32u + j < k) Dout[row * k + ch * 32u + j] = v[c2 * 32 + j] + x2;
         }
-        RefineEntry e{(uint32_t)row, (uint32_t)cls, i1, best.i2};
-        queue_refine(st, queue, valid && cls != 0, e);
+      }
+      ts->xmin[sub][r] = fminf(fminf(m0, m1), fminf(m2, m3));
+      mbar_arrive(&ts->x1[q]);
+      const bool ok1 = mbar_wait_bounded(&ts->x1[q], xp, abort_flag, WAIT_NS);
+      if (!__all_sync(0xffffffffu, ok1)) { if (lane == 0) fail(6); break; }
+      const float v1 = fminf(fminf(ts->xmin[0][r], ts->xmin[1][r]), fminf(ts->xmin[2][r], ts->xmin[3][r]));
+      // ---- pass 2: candidates v <= tau ----
+      const float tau = tie_tau(x2, v1, cmax, tb);
+      uint32_t cnt = 0, k0 = 0, k1 = 0, k2 = 0, k3 = 0;
+#pragma unroll
+      for (int c2 = 0; c2 < 2; ++c2) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const uint32_t col = ((uint32_t)sub + 4u * (uint32_t)c2) * 32u + (uint32_t)j;
+          if (v[c2 * 32 + j] <= tau && col < k) {
+            k0 = (cnt == 0) ? col : k0; k1 = (cnt == 1) ? col : k1;
+            k2 = (cnt == 2) ? col : k2; k3 = (cnt == 3) ? col : k3;
+            ++cnt;
+          }
+        }
+      }
+      // NaN anywhere (tau or v1) leaves cnt == 0: such a row takes the full path.
+      ts->xcnt[sub][r] = cnt;
+      ts->xcand[sub][r][0] = k0; ts->xcand[sub][r][1] = k1;
+      ts->xcand[sub][r][2] = k2; ts->xcand[sub][r][3] = k3;
+      mbar_arrive(&ts->x2[q]);
+      const bool ok2 = mbar_wait_bounded(&ts->x2[q], xp, abort_flag, WAIT_NS);
+      if (!__all_sync(0xffffffffu, ok2)) { if (lane == 0) fail(7); break; }
+      if (sub == 0) {
+        uint32_t total = 0, l0 = 0, l1 = 0, l2 = 0, l3 = 0, best = 0xffffffffu;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+          const uint32_t cw = ts->xcnt[w][r];
+#pragma unroll
+          for (uint32_t i = 0; i < 4; ++i) {
+            if (i < cw) {
+              const uint32_t c = ts->xcand[w][r][i];
+              const uint32_t pos = total + i;
+              l0 = (pos == 0) ? c : l0; l1 = (pos == 1) ? c : l1;
+              l2 = (pos == 2) ? c : l2; l3 = (pos == 3) ? c : l3;
+              best = min(best, c);
+            }
+          }
+          total += cw;
+        }
+        const bool valid = row < n;
+        if (valid) {
+          labels[row] = (total == 1) ? l0 : (best == 0xffffffffu ? 0u : best);
+          if (mindist) mindist[row] = v1 + x2;
+        }
+        RefineEntry e{(uint32_t)row, total, {l0, l1, l2, l3}};
+        const uint64_t seg = row >> 5;
+        seg_push(rq.cand, rq.ccnt, seg, valid && total >= 2 && total <= 4, e);
+        seg_push(rq.full, rq.fcnt, seg, valid && (total == 0 || total > 4), (uint32_t)row);
       }
     }
   }
@@ -252,7 +308,7 @@ TcPlan plan_tc(uint32_t dp, uint32_t kp, bool x3, uint64_t n, int num_sms) {
   const size_t mult = x3 ? 2 : 1;
   const size_t b_bytes = (size_t)p.KB * kp * 128 * mult;
   const size_t unit = (size_t)A_UNIT * mult;
-  const size_t fixed = 1024 /*align*/ + ((kp + 3) & ~3u) * 4 + sizeof(TcSmem) + 64;
+  const size_t fixed = 1024 /*align*/ + ((kp + 31) & ~31u) * 4 + sizeof(TcSmem) + 64;
   const size_t budget = 227 * 1024;
   if (b_bytes + fixed + 2 * unit > budget) return p;
   size_t s = (budget - b_bytes - fixed) / unit;
@@ -303,17 +359,17 @@ km_status launch_assign_tc(const TcPlan& pl, bool x3, const CUtensorMap& tmA,
                            const CUtensorMap& tmAlo, const CUtensorMap& tmB,
                            const CUtensorMap& tmBlo, const float* cn2, const float* xn2,
                            uint64_t n, uint32_t k, uint32_t kp, TieBound tb, DevState* st,
-                           uint32_t* labels, float* mindist, RefineEntry* queue, float* Dout,
-                           cudaStream_t s) {
+                           uint32_t* labels, float* mindist, const RefineQueues& rq,
+                           float* Dout, cudaStream_t s) {
   if (!pl.ok) return KM_ERR_UNSUPPORTED;
   if (x3) {
     assign_tc_kernel<true><<<pl.grid, TC_THREADS, pl.smem, s>>>(
         tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.KB, pl.stages, pl.nalloc, tb, st, labels,
-        mindist, queue, Dout);
+        mindist, rq, Dout);
   } else {
     assign_tc_kernel<false><<<pl.grid, TC_THREADS, pl.smem, s>>>(
         tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.KB, pl.stages, pl.nalloc, tb, st, labels,
-        mindist, queue, Dout);
+        mindist, rq, Dout);
   }
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
