@@ -176,6 +176,29 @@ km_status km_update(const float* X_dev, const uint32_t* labels_dev, uint64_t n, 
                     uint32_t k, float* C_dev, uint32_t* counts_dev, uint32_t* perm_dev,
                     uint32_t* offsets_dev, void* stream);
 
+/* km_update without any device allocation.  No counterpart in the reference:
+ * it exists for callers that cannot allocate device memory, such as hosts that
+ * own all device memory through their own pool and forbid cudaMalloc/cudaFree
+ * after start-up (those calls synchronise the device and fragment the pool),
+ * or latency-critical loops where an allocation is an unbounded stall.
+ *
+ * Same arithmetic and results as km_update (C and counts), but its scratch
+ * (label-sort counters and the label-sorted permutation) is one file-scope
+ * device array of KM_NOALLOC_SCRATCH_BYTES that every GPU loading the library
+ * holds until the process exits; it calls no cudaMalloc, cudaFree or other
+ * allocating routine.  Limits: n <= KM_NOALLOC_MAX_N and k <= KM_NOALLOC_MAX_K;
+ * larger sizes return KM_ERR_UNSUPPORTED before any work.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress, with that
+ * device current); make that first call before any stream capture.  Every call
+ * shares the array and the call clears what must start at zero: calls that
+ * overlap on the GPU (other streams or host threads) race and must not be
+ * issued.  counts_dev may be NULL. */
+#define KM_NOALLOC_MAX_N 1048576u
+#define KM_NOALLOC_MAX_K 1024u
+#define KM_NOALLOC_SCRATCH_BYTES 5505024u
+km_status km_update_noalloc(const float* X_dev, const uint32_t* labels_dev, uint64_t n, uint32_t d,
+                            uint32_t k, float* C_dev, uint32_t* counts_dev, void* stream);
+
 /* ---- Kernel k-means (popcorn formulation, src/kmeans.cu + distances.cu:895-1002) ---- */
 
 /* K = f(X X^T) (n*n row-major).  out_bf16 == 0 stores float32, 1 stores bf16.

@@ -71,6 +71,8 @@ SIGNATURES = {
                                C.c_void_p, C.c_void_p]),
     "km_update": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p,
                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "km_update_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]),
     "km_kernel_matrix": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, C.c_int32, C.c_float, C.c_float,
                                    C.c_int32, C.c_float, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                    C.c_void_p]),
