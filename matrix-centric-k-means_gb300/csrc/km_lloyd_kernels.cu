@@ -632,16 +632,19 @@ update_sums_kernel(const float* __restrict__ X, const uint32_t* __restrict__ per
   }
   // pq[i] holds the permutation indices of batch b + UPD_STAGES - 1 + i: the
   // load of a batch's indices is issued UPD_PREFETCH iterations before use.
+  // The loop is unrolled by UPD_PREFETCH so that pq[i] is consumed in place,
+  // UPD_PREFETCH batches after its load was issued.
   constexpr int UPD_PREFETCH = 8;
   uint32_t pq[UPD_PREFETCH];
 #pragma unroll
   for (int i = 0; i < UPD_PREFETCH; ++i) pq[i] = load_perm((uint32_t)(UPD_STAGES - 1 + i));
-  for (uint32_t b = 0; b < nb; ++b) {
-    const uint32_t cur = pq[0];
+  for (uint32_t b0 = 0; b0 < nb; b0 += UPD_PREFETCH)
 #pragma unroll
-    for (int i = 0; i + 1 < UPD_PREFETCH; ++i) pq[i] = pq[i + 1];
-    pq[UPD_PREFETCH - 1] = load_perm(b + UPD_STAGES - 1 + UPD_PREFETCH);
-    issue(b + UPD_STAGES - 1, cur);
+  for (int i = 0; i < UPD_PREFETCH; ++i) {
+    const uint32_t b = b0 + (uint32_t)i;
+    if (b >= nb) break;
+    issue(b + UPD_STAGES - 1, pq[i]);
+    pq[i] = load_perm(b + UPD_STAGES - 1 + UPD_PREFETCH);
     cp_async_wait<UPD_STAGES - 1>();
     __syncwarp();
     const uint32_t m = min((uint32_t)UPD_ROWS, s1 - (s0 + b * UPD_ROWS));
@@ -688,10 +691,163 @@ update_sums_kernel(const float* __restrict__ X, const uint32_t* __restrict__ per
   }
 }
 
+// Pipelined variant (d % 4 == 0, 16-byte aligned X): one CTA per (cluster,
+// 32-column block), so a cluster's d/32 column chains run on as many SMs and a
+// large cluster is not bound to one SM's outstanding-request capacity.  Warp 0
+// produces: 16-byte cp.async per lane, one instruction copying BLK_RPI row
+// segments, into a BLK_STAGES-deep ring; arrival on the stage's mbarrier fires
+// when its copies land (cp.async.mbarrier.arrive.noinc).  Warp 1 consumes,
+// lane = column: a full batch is loaded into registers first, then summed in
+// row order exactly as the reference (kmeans.cpp:133-137).  Every wait is
+// bounded; on timeout the CTA flags KM_DEVERR_TIMEOUT and drains its copies
+// before exiting.  Permutation indices are prefetched P batches ahead in
+// registers consumed in place.
+namespace {
+constexpr int BLK_ROWS = 32, BLK_STAGES = 8, BLK_COLS = 32;
+constexpr uint64_t BLK_WAIT_NS = 2000000000ull;
+constexpr size_t BLK_SMEM = (size_t)BLK_STAGES * BLK_ROWS * BLK_COLS * sizeof(float);
+constexpr int BLK_LPR = BLK_COLS / 4;           // lanes per row (16 bytes each)
+constexpr int BLK_RPI = 32 / BLK_LPR;           // rows per copy instruction
+}  // namespace
+
+__global__ void __launch_bounds__(32 * (1 + BLK_COLS / 32))
+update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict__ perm,
+                        const uint32_t* __restrict__ cstart, uint32_t d, uint32_t k,
+                        const float* __restrict__ C, float* __restrict__ Cn,
+                        float* __restrict__ dsq, double* __restrict__ objpart, DevState* st) {
+  if (st && st->done) return;
+  extern __shared__ __align__(128) float ring[];        // [BLK_STAGES][BLK_ROWS][BLK_COLS]
+  __shared__ __align__(8) uint64_t full[BLK_STAGES], empty[BLK_STAGES];
+  __shared__ int abort_flag;
+  const uint32_t nblk = (d + BLK_COLS - 1) / BLK_COLS;
+  const uint32_t c = blockIdx.x / nblk, j0 = (blockIdx.x % nblk) * BLK_COLS;
+  const uint32_t w = min((uint32_t)BLK_COLS, d - j0);   // columns of this block (multiple of 4)
+  const uint32_t nc = (w + 31) / 32;                    // consumer warps doing work
+  const uint32_t s0 = cstart[c], s1 = cstart[c + 1];
+  const uint32_t nb = (s1 - s0 + BLK_ROWS - 1) / BLK_ROWS;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < BLK_STAGES; ++s) { mbar_init(&full[s], 32); mbar_init(&empty[s], nc); }
+    abort_flag = 0;
+    mbar_fence_init();
+  }
+  __syncthreads();
+  volatile int* ab = &abort_flag;
+  auto fail = [&]() {
+    abort_flag = 1;
+    if (st) atomicOr(&st->err, KM_DEVERR_TIMEOUT);
+  };
+
+  if (warp == 0) {
+    constexpr int P = 8;
+    uint32_t pq[P];
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+      const uint32_t idx = s0 + (uint32_t)i * BLK_ROWS + (uint32_t)lane;
+      pq[i] = ((uint32_t)i < nb && idx < s1) ? perm[idx] : 0u;
+    }
+    // Unrolled by P so that pq[i] is consumed in place, P batches after its
+    // load was issued (moving a register whose load is in flight would wait).
+    uint32_t issued = 0;
+    bool ok = true;
+    for (uint32_t b0 = 0; b0 < nb && ok; b0 += P) {
+#pragma unroll
+      for (int i = 0; i < P; ++i) {
+        const uint32_t b = b0 + (uint32_t)i;
+        if (b >= nb || !ok) break;
+        const uint32_t s = b % BLK_STAGES, ph = (b / BLK_STAGES) & 1u;
+        const bool okw = mbar_wait_bounded(&empty[s], ph ^ 1u, ab, BLK_WAIT_NS);
+        if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(); ok = false; break; }
+        const uint32_t m = min((uint32_t)BLK_ROWS, s1 - (s0 + b * BLK_ROWS));
+        const uint32_t rl = pq[i];
+        // One instruction copies BLK_RPI rows: BLK_LPR lanes of 16 bytes per
+        // row; columns past w and rows past m zero-fill.
+        const uint32_t sub = (uint32_t)lane / BLK_LPR, c4 = ((uint32_t)lane % BLK_LPR) * 4u;
+        const bool lane_has_cols = c4 < w;
+        float* dst = ring + ((size_t)s * BLK_ROWS + sub) * BLK_COLS + c4;
+        // All row indices first: each cp.async is an ordered asm statement, so
+        // a shuffle placed between two of them would put its latency on every row.
+        uint32_t rr[BLK_ROWS / BLK_RPI];
+#pragma unroll
+        for (int ii = 0; ii < BLK_ROWS / BLK_RPI; ++ii)
+          rr[ii] = __shfl_sync(0xffffffffu, rl, ii * BLK_RPI + (int)sub);
+        const float* xl = X + j0 + c4;
+#pragma unroll
+        for (int ii = 0; ii < BLK_ROWS / BLK_RPI; ++ii) {
+          const uint32_t u = (uint32_t)ii * BLK_RPI + sub;
+          const bool okr = u < m && lane_has_cols;
+          const float* src = okr ? xl + (uint64_t)rr[ii] * d : X;
+          cp_async16_zfill(dst + (size_t)ii * BLK_RPI * BLK_COLS, src, okr ? 16u : 0u);
+        }
+        cp_async_mbar_arrive_noinc(&full[s]);
+        const uint32_t nbb = b + P;
+        const uint32_t idx = s0 + nbb * BLK_ROWS + (uint32_t)lane;
+        pq[i] = (nbb < nb && idx < s1) ? perm[idx] : 0u;
+        issued = b + 1;
+      }
+    }
+    // Drain: this warp's copies must land before the CTA exits.
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    (void)issued;
+  } else if ((uint32_t)warp <= nc) {
+    const uint32_t col = (uint32_t)(warp - 1) * 32u + (uint32_t)lane;   // column within the block
+    const bool vj = col < w;
+    const uint64_t p = (uint64_t)c * d + j0 + col;
+    const float cold = (C && vj) ? C[p] : 0.0f;
+    float sum = 0.0f;
+    double e64 = 0.0;
+    for (uint32_t b = 0; b < nb; ++b) {
+      const uint32_t s = b % BLK_STAGES, ph = (b / BLK_STAGES) & 1u;
+      const bool ok = mbar_wait_bounded(&full[s], ph, ab, BLK_WAIT_NS);
+      if (!__all_sync(0xffffffffu, ok)) { if (lane == 0) fail(); break; }
+      const uint32_t m = min((uint32_t)BLK_ROWS, s1 - (s0 + b * BLK_ROWS));
+      const float* src = ring + (size_t)s * BLK_ROWS * BLK_COLS + col;
+      float e32 = 0.0f, e32b = 0.0f;
+      if (m == (uint32_t)BLK_ROWS) {
+        // Full batch: all loads first, then the ordered chain (no branch or
+        // load latency on the dependent additions).
+        float v[BLK_ROWS];
+#pragma unroll
+        for (int u = 0; u < BLK_ROWS; ++u) v[u] = vj ? src[(size_t)u * BLK_COLS] : 0.0f;
+#pragma unroll
+        for (int u = 0; u < BLK_ROWS; ++u) {
+          sum = __fadd_rn(sum, v[u]);
+          const float t = v[u] - cold;
+          if (u & 1) e32b = fmaf(t, t, e32b); else e32 = fmaf(t, t, e32);
+        }
+      } else {
+        for (uint32_t u = 0; u < m; ++u) {
+          const float v = vj ? src[(size_t)u * BLK_COLS] : 0.0f;
+          sum = __fadd_rn(sum, v);
+          const float t = v - cold;
+          e32 = fmaf(t, t, e32);
+        }
+      }
+      e32 += e32b;
+      e64 += e32;
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+    }
+    if (vj) {
+      const uint32_t cnt = s1 - s0;
+      const float scale = __double2float_rn(1.0 / (double)(cnt > 1 ? cnt : 1));
+      const float cn = __fmul_rn(sum, scale);
+      Cn[p] = cn;
+      if (dsq) {
+        const float t = __fsub_rn(cn, cold);
+        dsq[p] = __fmul_rn(t, t);
+      }
+      if (objpart) objpart[p] = e64;
+    }
+  }
+}
+
 // Opt-in shared memory for the VEC = 4 ring; called before any capture.
 km_status update_sums_prepare() {
   KM_CUDA_TRY(cudaFuncSetAttribute(update_sums_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    UPD_STAGES * UPD_ROWS * 128 * (int)sizeof(float)));
+  KM_CUDA_TRY(cudaFuncSetAttribute(update_sums_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)BLK_SMEM));
   return KM_OK;
 }
 
@@ -702,8 +858,14 @@ km_status update_sums_prepare() {
 km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_t* cstart, uint32_t d,
                              uint32_t k, const float* C, float* Cn, float* dsq, double* objpart,
                              DevState* st, cudaStream_t s) {
-  const bool v4 = (d % 4 == 0) && (reinterpret_cast<uintptr_t>(X) % 16 == 0) &&
-                  (uint64_t)k * ((d + 127) / 128) >= 4096;
+  if (d % 4 == 0 && reinterpret_cast<uintptr_t>(X) % 16 == 0) {
+    const uint64_t ctas = (uint64_t)k * ((d + BLK_COLS - 1) / BLK_COLS);
+    update_sums_bulk_kernel<<<(unsigned)ctas, 32 * (1 + BLK_COLS / 32), BLK_SMEM, s>>>(
+        X, perm, cstart, d, k, C, Cn, dsq, objpart, st);
+    KM_CUDA_TRY(cudaGetLastError());
+    return KM_OK;
+  }
+  const bool v4 = false;
   const uint32_t W = v4 ? 128u : 32u;
   const uint64_t warps = (uint64_t)k * ((d + W - 1) / W);
   const size_t smem = (size_t)UPD_STAGES * UPD_ROWS * W * sizeof(float);

@@ -11,15 +11,16 @@
 //   warp 0       TMA producer (one elected lane)
 //   warp 1       MMA issuer (one elected lane)
 //   warp 2       TMEM allocator
-//   warps 4-19   epilogue, four warps per TMEM lane quadrant (warp w reads
-//                lanes 32*(w%4)..+31), each on a quarter of the column chunks:
-//                pass 1  v = ||c||^2 - 2 acc kept in registers, row minimum v1;
-//                        the TMEM buffer is released right after the loads;
-//                pass 2  candidates {c : v(c) <= tau(v1)} (tie_tau); one
-//                        candidate: the label is proven; 2..4: queued for the
-//                        exact re-score of those; more: full re-score.
-//                The four warps of a quadrant combine through shared memory
-//                with bounded mbarrier hand-offs.
+//   warps 4-11   epilogue, two sets of four warps: set s takes the tiles
+//                t = s (mod 2), i.e. TMEM accumulator buffer s, so two tiles
+//                are in the epilogue at once; warp w reads TMEM lanes
+//                32*(w%4)..+31 (its rows) across all kp columns, with no
+//                exchange between warps:
+//                pass 1  row minimum v1 of v = ||c||^2 - 2 acc;
+//                pass 2  candidates {c : v(c) <= tau(v1)} (tie_tau) as
+//                        per-chunk bit masks (TMEM is read a second time);
+//                one candidate: the label is proven; 2..4: queued for the
+//                exact re-score of those; more: full re-score.
 //
 // Every mbarrier wait is bounded (2 s); on timeout the CTA raises an abort
 // flag, records KM_DEVERR_TIMEOUT, waits (bounded) for its own copies and MMAs
@@ -39,7 +40,7 @@ namespace km {
 
 namespace {
 
-constexpr int TC_EPI_WARPS = 16;
+constexpr int TC_EPI_WARPS = 8;
 constexpr int TC_THREADS = 32 * (4 + TC_EPI_WARPS);
 constexpr int TC_M = 128;
 constexpr uint64_t WAIT_NS = 2000000000ull;
@@ -52,13 +53,8 @@ struct TcSmem {
   uint64_t tfull[2];
   uint64_t tempty[2];
   uint64_t tdone;
-  uint64_t x1[4];     // per quadrant: partial minima written
-  uint64_t x2[4];     // per quadrant: partial candidate lists written
   uint32_t tmem_base;
   int abort;
-  float xmin[4][TC_M];
-  uint32_t xcnt[4][TC_M];
-  uint32_t xcand[4][TC_M][4];
 };
 
 template <bool X3>
@@ -78,7 +74,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   uint8_t* sA = smem + b_bytes * (X3 ? 2u : 1u);
   const uint32_t unit_bytes = A_UNIT * (X3 ? 2u : 1u);
   float* cns = reinterpret_cast<float*>(sA + (size_t)S * unit_bytes);
-  TcSmem* ts = reinterpret_cast<TcSmem*>(cns + ((kp + 31) & ~31u));
+  TcSmem* ts = reinterpret_cast<TcSmem*>(cns + ((kp + 63) & ~63u));
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t ntiles = (n + TC_M - 1) / TC_M;
@@ -87,14 +83,13 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   if (threadIdx.x == 0) {
     for (uint32_t s = 0; s < S; ++s) { mbar_init(&ts->full[s], 1); mbar_init(&ts->empty[s], 1); }
     mbar_init(&ts->bfull, 1);
-    for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], TC_EPI_WARPS); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], 4); }
     mbar_init(&ts->tdone, 1);
-    for (int q = 0; q < 4; ++q) { mbar_init(&ts->x1[q], 128); mbar_init(&ts->x2[q], 128); }
     ts->abort = 0;
     mbar_fence_init();
   }
-  const uint32_t kp32 = (kp + 31) & ~31u;
-  for (uint32_t c = threadIdx.x; c < kp32; c += blockDim.x)
+  const uint32_t kp64 = (kp + 63) & ~63u;    // +inf padding up to whole 64-column loads
+  for (uint32_t c = threadIdx.x; c < kp64; c += blockDim.x)
     cns[c] = (c < k) ? cn2[c] : __int_as_float(0x7f800000);
   if (warp == 2) tmem_alloc(&ts->tmem_base, 2u * nalloc);
   tc_fence_before();
@@ -186,110 +181,98 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       }
     }
   } else if (warp >= 4) {
-    const int q = warp & 3, sub = (warp - 4) >> 2;
-    const uint32_t nch = (kp + 31) / 32;            // <= 8, so <= 2 chunks per warp
+    // Epilogue set `set` (0/1) takes the tiles with t % 2 == set, i.e. TMEM
+    // accumulator buffer `set`; warp q = warp % 4 owns TMEM lanes (rows)
+    // 32q..32q+31 and all kp columns of them, so no cross-warp exchange.
+    const int q = warp & 3, set = (warp - 4) >> 2;
+    const uint32_t npair = (kp + 63) / 64;          // <= 4 loads of 64 columns
     const uint32_t r = (uint32_t)q * 32u + (uint32_t)lane;
-    uint64_t t = 0;
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
-      const uint32_t buf = (uint32_t)(t & 1u), use = (uint32_t)(t >> 1), xp = (uint32_t)(t & 1u);
-      const bool okw = mbar_wait_bounded(&ts->tfull[buf], use & 1u, abort_flag, WAIT_NS);
-      if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(5); break; }
-      tc_fence_after();
+    const uint32_t tbase = tmem_base + (((uint32_t)q * 32u) << 16) + (uint32_t)set * nalloc;
+    uint64_t t = (uint64_t)set;
+    for (uint64_t tile = blockIdx.x + (uint64_t)set * gridDim.x; tile < ntiles;
+         tile += 2ull * gridDim.x, t += 2) {
+      const uint32_t use = (uint32_t)(t >> 1);
       const uint64_t row = tile * TC_M + r;
       const float x2 = (row < n) ? xn2[row] : 0.0f;
-      // ---- pass 1: values into registers, row minimum ----
-      float v[64];
+      const bool okw = mbar_wait_bounded(&ts->tfull[set], use & 1u, abort_flag, WAIT_NS);
+      if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(5); break; }
+      tc_fence_after();
+      // ---- pass 1: row minimum of v = ||c||^2 - 2 acc (64 columns per load) ----
       float m0 = __int_as_float(0x7f800000), m1 = m0, m2 = m0, m3 = m0;
+      for (uint32_t pr = 0; pr < npair; ++pr) {
+        uint32_t acc[64];
+        tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
+        tmem_ld_wait();
+        const float4* cn4 = reinterpret_cast<const float4*>(cns + pr * 64u);
 #pragma unroll
-      for (int c2 = 0; c2 < 2; ++c2) {
-        const uint32_t ch = (uint32_t)sub + 4u * (uint32_t)c2;
-        if (ch < nch) {
-          uint32_t acc[32];
-          tmem_ld_32x32b_x32(tmem_base + (((uint32_t)q * 32u) << 16) + buf * nalloc + ch * 32u, acc);
-          tmem_ld_wait();
-          const float4* cn4 = reinterpret_cast<const float4*>(cns + ch * 32u);
+        for (int j4 = 0; j4 < 16; ++j4) {
+          const float4 cc = cn4[j4];
+          m0 = fminf(m0, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 0]), cc.x));
+          m1 = fminf(m1, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 1]), cc.y));
+          m2 = fminf(m2, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 2]), cc.z));
+          m3 = fminf(m3, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 3]), cc.w));
+        }
+      }
+      const float v1 = fminf(fminf(m0, m1), fminf(m2, m3));
+      const float tau = tie_tau(x2, v1, cmax, tb);
+      // ---- pass 2: candidates {c < k : v(c) <= tau}, as 32-column bit masks ----
+      uint32_t cnt = 0, got = 0, k0 = 0, k1 = 0, k2 = 0, k3 = 0;
+      for (uint32_t pr = 0; pr < npair; ++pr) {
+        uint32_t acc[64];
+        tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
+        tmem_ld_wait();
+        const float4* cn4 = reinterpret_cast<const float4*>(cns + pr * 64u);
+        uint32_t mlo = 0, mhi = 0;
 #pragma unroll
-          for (int j4 = 0; j4 < 8; ++j4) {
-            const float4 cc = cn4[j4];
-            const float a = fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 0]), cc.x);
-            const float b = fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 1]), cc.y);
-            const float c = fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 2]), cc.z);
-            const float e = fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 3]), cc.w);
-            v[c2 * 32 + 4 * j4 + 0] = a; v[c2 * 32 + 4 * j4 + 1] = b;
-            v[c2 * 32 + 4 * j4 + 2] = c; v[c2 * 32 + 4 * j4 + 3] = e;
-            m0 = fminf(m0, a); m1 = fminf(m1, b); m2 = fminf(m2, c); m3 = fminf(m3, e);
+        for (int j4 = 0; j4 < 8; ++j4) {
+          const float4 cc = cn4[j4];
+          if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 0]), cc.x) <= tau) mlo |= 1u << (4 * j4 + 0);
+          if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 1]), cc.y) <= tau) mlo |= 1u << (4 * j4 + 1);
+          if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 2]), cc.z) <= tau) mlo |= 1u << (4 * j4 + 2);
+          if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 3]), cc.w) <= tau) mlo |= 1u << (4 * j4 + 3);
+        }
+#pragma unroll
+        for (int j4 = 0; j4 < 8; ++j4) {
+          const float4 cc = cn4[8 + j4];
+          if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 0]), cc.x) <= tau) mhi |= 1u << (4 * j4 + 0);
+          if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 1]), cc.y) <= tau) mhi |= 1u << (4 * j4 + 1);
+          if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 2]), cc.z) <= tau) mhi |= 1u << (4 * j4 + 2);
+          if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 3]), cc.w) <= tau) mhi |= 1u << (4 * j4 + 3);
+        }
+        uint32_t mm[2] = {mlo, mhi};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t c0 = pr * 64u + (uint32_t)h * 32u;
+          uint32_t m = mm[h] & ((c0 >= k) ? 0u : (k - c0 >= 32u ? 0xffffffffu : ((1u << (k - c0)) - 1u)));
+          cnt += (uint32_t)__popc(m);
+          while (m != 0u && got < 4u) {
+            const uint32_t col = c0 + (uint32_t)(__ffs(m) - 1);
+            m &= m - 1u;
+            k0 = (got == 0) ? col : k0; k1 = (got == 1) ? col : k1;
+            k2 = (got == 2) ? col : k2; k3 = (got == 3) ? col : k3;
+            ++got;
           }
-        } else {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) v[c2 * 32 + j] = __int_as_float(0x7f800000);
+        }
+        if (Dout && row < n) {
+          for (int j = 0; j < 64; ++j)
+            if (pr * 64u + j < k)
+              Dout[row * k + pr * 64u + j] = fmaf(-2.0f, __uint_as_float(acc[j]), cns[pr * 64u + j]) + x2;
         }
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&ts->tempty[buf]);     // accumulator buffer free
-      if (Dout && row < n) {
-#pragma unroll
-        for (int c2 = 0; c2 < 2; ++c2) {
-          const uint32_t ch = (uint32_t)sub + 4u * (uint32_t)c2;
-          if (ch < nch)
-            for (int j = 0; j < 32; ++j)
-              if (ch * 32u + j < k) Dout[row * k + ch * 32u + j] = v[c2 * 32 + j] + x2;
-        }
-      }
-      ts->xmin[sub][r] = fminf(fminf(m0, m1), fminf(m2, m3));
-      mbar_arrive(&ts->x1[q]);
-      const bool ok1 = mbar_wait_bounded(&ts->x1[q], xp, abort_flag, WAIT_NS);
-      if (!__all_sync(0xffffffffu, ok1)) { if (lane == 0) fail(6); break; }
-      const float v1 = fminf(fminf(ts->xmin[0][r], ts->xmin[1][r]), fminf(ts->xmin[2][r], ts->xmin[3][r]));
-      // ---- pass 2: candidates v <= tau ----
-      const float tau = tie_tau(x2, v1, cmax, tb);
-      uint32_t cnt = 0, k0 = 0, k1 = 0, k2 = 0, k3 = 0;
-#pragma unroll
-      for (int c2 = 0; c2 < 2; ++c2) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const uint32_t col = ((uint32_t)sub + 4u * (uint32_t)c2) * 32u + (uint32_t)j;
-          if (v[c2 * 32 + j] <= tau && col < k) {
-            k0 = (cnt == 0) ? col : k0; k1 = (cnt == 1) ? col : k1;
-            k2 = (cnt == 2) ? col : k2; k3 = (cnt == 3) ? col : k3;
-            ++cnt;
-          }
-        }
-      }
+      if (lane == 0) mbar_arrive(&ts->tempty[set]);      // accumulator buffer free
+      // Candidates come out in ascending column order: k0 is the lowest index.
       // NaN anywhere (tau or v1) leaves cnt == 0: such a row takes the full path.
-      ts->xcnt[sub][r] = cnt;
-      ts->xcand[sub][r][0] = k0; ts->xcand[sub][r][1] = k1;
-      ts->xcand[sub][r][2] = k2; ts->xcand[sub][r][3] = k3;
-      mbar_arrive(&ts->x2[q]);
-      const bool ok2 = mbar_wait_bounded(&ts->x2[q], xp, abort_flag, WAIT_NS);
-      if (!__all_sync(0xffffffffu, ok2)) { if (lane == 0) fail(7); break; }
-      if (sub == 0) {
-        uint32_t total = 0, l0 = 0, l1 = 0, l2 = 0, l3 = 0, best = 0xffffffffu;
-#pragma unroll
-        for (int w = 0; w < 4; ++w) {
-          const uint32_t cw = ts->xcnt[w][r];
-#pragma unroll
-          for (uint32_t i = 0; i < 4; ++i) {
-            if (i < cw) {
-              const uint32_t c = ts->xcand[w][r][i];
-              const uint32_t pos = total + i;
-              l0 = (pos == 0) ? c : l0; l1 = (pos == 1) ? c : l1;
-              l2 = (pos == 2) ? c : l2; l3 = (pos == 3) ? c : l3;
-              best = min(best, c);
-            }
-          }
-          total += cw;
-        }
-        const bool valid = row < n;
-        if (valid) {
-          labels[row] = (total == 1) ? l0 : (best == 0xffffffffu ? 0u : best);
-          if (mindist) mindist[row] = v1 + x2;
-        }
-        RefineEntry e{(uint32_t)row, total, {l0, l1, l2, l3}};
-        const uint64_t seg = row >> 5;
-        seg_push(rq.cand, rq.ccnt, seg, valid && total >= 2 && total <= 4, e);
-        seg_push(rq.full, rq.fcnt, seg, valid && (total == 0 || total > 4), (uint32_t)row);
+      const bool valid = row < n;
+      if (valid) {
+        labels[row] = k0;
+        if (mindist) mindist[row] = v1 + x2;
       }
+      RefineEntry e{(uint32_t)row, cnt, {k0, k1, k2, k3}};
+      const uint64_t seg = row >> 5;
+      seg_push(rq.cand, rq.ccnt, seg, valid && cnt >= 2 && cnt <= 4, e);
+      seg_push(rq.full, rq.fcnt, seg, valid && (cnt == 0 || cnt > 4), (uint32_t)row);
     }
   }
 
@@ -308,13 +291,13 @@ TcPlan plan_tc(uint32_t dp, uint32_t kp, bool x3, uint64_t n, int num_sms) {
   const size_t mult = x3 ? 2 : 1;
   const size_t b_bytes = (size_t)p.KB * kp * 128 * mult;
   const size_t unit = (size_t)A_UNIT * mult;
-  const size_t fixed = 1024 /*align*/ + ((kp + 31) & ~31u) * 4 + sizeof(TcSmem) + 64;
+  const size_t fixed = 1024 /*align*/ + ((kp + 63) & ~63u) * 4 + sizeof(TcSmem) + 64;
   const size_t budget = 227 * 1024;
   if (b_bytes + fixed + 2 * unit > budget) return p;
   size_t s = (budget - b_bytes - fixed) / unit;
   if (s > 8) s = 8;
   p.stages = (uint32_t)s;
-  p.nalloc = 32;
+  p.nalloc = 64;                 // >= 64: a 64-column TMEM load never leaves the buffer
   while (p.nalloc < kp) p.nalloc <<= 1;
   p.smem = b_bytes + fixed + s * unit;
   const uint64_t ntiles = (n + TC_M - 1) / TC_M;
