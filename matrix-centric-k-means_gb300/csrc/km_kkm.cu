@@ -1,33 +1,741 @@
-// Kernel k-means (popcorn formulation): kernel-matrix build and iteration.
+// Kernel k-means for sm_103a (the reference's current "popcorn" GPU path).
+//
+//  (a) kernel matrix  K = f(X X^T)  (src/kernels/kernels.cuh:43-118, :568-718):
+//      tcgen05 GEMM (BF16 or split-BF16x3 operands, FP32 accumulators in TMEM,
+//      TMA-fed) or SIMT FP32 GEMM, with the kernel function applied in the
+//      epilogue and K (and diag K) stored once.  The reference stores
+//      B = -2 f(.) and runs an n^2 Thrust pass; here f is fused and the -2 is
+//      folded into the distance.
+//  (c) one iteration (src/kmeans.cu:772-1073, src/kernels/distances.cu:895-1002):
+//      E = K V^T streamed over the rows of K once (E[i,c] = sum_{j in c} K_ij,
+//      per-lane shared-memory bins, deterministic order), ctilde_c =
+//      (1/|c|^2) sum_{i in c} E[i,c] = diag(V K V^T) in FP64 over the
+//      label-sorted permutation, then D[i,c] = -2 E[i,c]/|c| + ctilde_c
+//      (ctilde_c == 0 -> +inf, distances.cu:588-599), argmin keeping the lowest
+//      index from (0, FLT_MAX) (kmeans.cu:923-936), score = sum_i min_c D
+//      (kmeans.cu:1054-1061; it leaves out K_ii), stop on |score - last| < tol
+//      from iteration 2 when checking (kmeans.cu:1064-1073).
 #include "km_lloyd.cuh"
+
+#include <cudaTypedefs.h>
+#include <cmath>
+#include <cstring>
+#include <cfloat>
+#include <new>
+
+namespace km {
+
+__global__ void round_robin_labels_kernel(uint32_t* labels, uint64_t n, uint32_t k);  // km_capi.cu
+
+struct KFn {
+  int kind;        // km_kernel_fn
+  float gamma, coef, inv2s2;
+  int degree;
+};
+
+__device__ __forceinline__ float kfn_apply(const KFn& f, float dot, float ni, float nj) {
+  switch (f.kind) {
+    case KM_KERNEL_LINEAR: return dot;
+    case KM_KERNEL_POLY: {
+      const float b = fmaf(f.gamma, dot, f.coef);
+      float r = 1.0f;
+      for (int e = 0; e < f.degree; ++e) r *= b;
+      return r;
+    }
+    case KM_KERNEL_SIGMOID: return tanhf(fmaf(f.gamma, dot, f.coef));
+    default: {
+      const float d2 = fmaxf(ni + nj - 2.0f * dot, 0.0f);
+      return expf(-d2 * f.inv2s2);
+    }
+  }
+}
+
+// ||x_i||^2 of the operands the tensor cores see (hi, or hi + lo): the
+// Gaussian epilogue's ||x_i||^2 + ||x_j||^2 - 2 x_i.x_j is then the squared
+// distance of those operands (K_ii = 1 exactly), instead of mixing FP32 norms
+// with a BF16 dot product.
+__global__ void kmat_operand_norms_kernel(const __nv_bfloat16* __restrict__ Xb,
+                                          const __nv_bfloat16* __restrict__ Xlo, uint64_t n,
+                                          uint32_t dp, float* __restrict__ out) {
+  const uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  double s = 0.0;
+  for (uint32_t j = lane; j < dp; j += 32) {
+    float v = __bfloat162float(Xb[r * dp + j]);
+    if (Xlo) v += __bfloat162float(Xlo[r * dp + j]);
+    s += (double)v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[r] = (float)s;
+}
+
+template <bool OUT_BF16>
+__device__ __forceinline__ void kstore(void* K, uint64_t idx, float v) {
+  if (OUT_BF16) reinterpret_cast<__nv_bfloat16*>(K)[idx] = __float2bfloat16_rn(v);
+  else reinterpret_cast<float*>(K)[idx] = v;
+}
+
+// ---------------------------------------------------------------------------
+// (a) SIMT FP32 kernel-matrix GEMM: 128 x 128 tiles, 256 threads, 8 x 8
+// micro-tiles, K chunks of 16 through shared memory.
+// ---------------------------------------------------------------------------
+template <bool OUT_BF16>
+__global__ void __launch_bounds__(256)
+kmat_f32_kernel(const float* __restrict__ X, const float* __restrict__ xn2, uint64_t n, uint32_t d,
+                KFn f, void* __restrict__ K, float* __restrict__ diag) {
+  __shared__ __align__(16) float As[16][128 + 4];
+  __shared__ __align__(16) float Bs[16][128 + 4];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const uint64_t m0 = (uint64_t)blockIdx.y * 128, c0 = (uint64_t)blockIdx.x * 128;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+  for (uint32_t kc = 0; kc < d; kc += 16) {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int idx = e * 256 + tid;
+      const int r = idx >> 4, kk = idx & 15;
+      const uint32_t col = kc + kk;
+      As[kk][r] = (m0 + r < n && col < d) ? X[(m0 + r) * d + col] : 0.0f;
+      Bs[kk][r] = (c0 + r < n && col < d) ? X[(c0 + r) * d + col] : 0.0f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      float a[8], b[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) { a[i] = As[kk][ty * 8 + i]; b[i] = Bs[kk][tx * 8 + i]; }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const uint64_t row = m0 + ty * 8 + i;
+    if (row >= n) continue;
+    const float ni = xn2[row];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint64_t col = c0 + tx * 8 + j;
+      if (col >= n) continue;
+      const float v = kfn_apply(f, acc[i][j], ni, xn2[col]);
+      kstore<OUT_BF16>(K, row * n + col, v);
+      if (diag && row == col) diag[row] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// (a) tcgen05 kernel-matrix GEMM.  Persistent CTAs walk 128 x 256 output
+// tiles; per K-block the A tile (128 rows) and B tile (256 rows) of the BF16
+// copy of X (hi, and lo for X3) come in by TMA into a ring of stages; one
+// thread issues the MMAs into a TMEM accumulator (two buffers of 256
+// columns); eight epilogue warps (two sets, one per buffer; warp w on TMEM
+// lanes 32*(w%4)) read the accumulator 64 columns at a time, apply f and store
+// K.  Every wait is bounded (2 s) and a timeout raises KM_DEVERR_TIMEOUT after
+// draining this CTA's copies and MMAs.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int KM_M = 128, KM_N = 256;
+constexpr uint32_t KA_BYTES = KM_M * 128;   // 64-column BF16 K-block of A
+constexpr uint32_t KB_BYTES = KM_N * 128;   // 64-column BF16 K-block of B
+constexpr uint64_t KWAIT_NS = 2000000000ull;
+
+struct KmSmem {
+  uint64_t full[8];
+  uint64_t empty[8];
+  uint64_t tfull[2];
+  uint64_t tempty[2];
+  uint64_t tdone;
+  uint32_t tmem_base;
+  int abort;
+};
+}  // namespace
+
+template <bool X3, bool OUT_BF16>
+__global__ void __launch_bounds__(384, 1)
+kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tAlo,
+               const __grid_constant__ CUtensorMap tB, const __grid_constant__ CUtensorMap tBlo,
+               const float* __restrict__ xn2, uint64_t n, uint32_t KB, uint32_t S, KFn f,
+               void* __restrict__ K, float* __restrict__ diag, int vec, DevState* st) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  const uint32_t stage_bytes = (KA_BYTES + KB_BYTES) * (X3 ? 2u : 1u);
+  KmSmem* ts = reinterpret_cast<KmSmem*>(smem + (size_t)S * stage_bytes);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint64_t mt = (n + KM_M - 1) / KM_M, nt = (n + KM_N - 1) / KM_N;
+  const uint64_t ntiles = mt * nt;
+  if (threadIdx.x == 0) {
+    for (uint32_t s = 0; s < S; ++s) { mbar_init(&ts->full[s], 1); mbar_init(&ts->empty[s], 1); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], 4); }
+    mbar_init(&ts->tdone, 1);
+    ts->abort = 0;
+    mbar_fence_init();
+  }
+  if (warp == 2) tmem_alloc(&ts->tmem_base, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = ts->tmem_base;
+  volatile int* abort_flag = &ts->abort;
+  auto fail = [&](uint32_t where) {
+    ts->abort = 1;
+    if (atomicOr(&st->err, KM_DEVERR_TIMEOUT) == 0u) st->err_where = 100u + where;
+  };
+  // tile t -> (mi, nj), row tiles outermost so that B tiles are reused from L2
+  if (warp == 0) {
+    if (lane == 0) {
+      uint64_t u = 0;
+      bool ok = true;
+      for (uint64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const uint64_t mi = tile / nt, nj = tile % nt;
+        for (uint32_t kb = 0; kb < KB; ++kb, ++u) {
+          const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
+          if (!mbar_wait_bounded(&ts->empty[s], ph ^ 1u, abort_flag, KWAIT_NS)) { fail(1); ok = false; break; }
+          mbar_arrive_expect_tx(&ts->full[s], stage_bytes);
+          uint8_t* dst = smem + (size_t)s * stage_bytes;
+          tma_load_2d(dst, &tA, (int)(kb * 64), (int)(mi * KM_M), &ts->full[s]);
+          tma_load_2d(dst + KA_BYTES, &tB, (int)(kb * 64), (int)(nj * KM_N), &ts->full[s]);
+          if (X3) {
+            tma_load_2d(dst + KA_BYTES + KB_BYTES, &tAlo, (int)(kb * 64), (int)(mi * KM_M), &ts->full[s]);
+            tma_load_2d(dst + 2 * KA_BYTES + KB_BYTES, &tBlo, (int)(kb * 64), (int)(nj * KM_N), &ts->full[s]);
+          }
+        }
+      }
+      volatile int no_abort = 0;
+      const uint64_t first = u > S ? u - S : 0;
+      for (uint64_t v = first; v < u; ++v)
+        mbar_wait_bounded(&ts->full[v % S], (uint32_t)((v / S) & 1u), &no_abort, KWAIT_NS);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(KM_M, KM_N);
+      const uint32_t s0 = smem_u32(smem);
+      uint64_t u = 0, t = 0;
+      bool ok = true, issued = false;
+      for (uint64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++t) {
+        const uint32_t buf = (uint32_t)(t & 1u), use = (uint32_t)(t >> 1);
+        if (!mbar_wait_bounded(&ts->tempty[buf], (use & 1u) ^ 1u, abort_flag, KWAIT_NS)) { fail(2); ok = false; break; }
+        tc_fence_after();
+        const uint32_t dt = tmem_base + buf * 256u;
+        for (uint32_t kb = 0; kb < KB; ++kb, ++u) {
+          const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
+          if (!mbar_wait_bounded(&ts->full[s], ph, abort_flag, KWAIT_NS)) { fail(3); ok = false; break; }
+          tc_fence_after();
+          const uint32_t a0 = s0 + s * stage_bytes, b0 = a0 + KA_BYTES;
+#pragma unroll
+          for (uint32_t kk = 0; kk < 4; ++kk) {
+            const uint64_t ad = smem_desc_sw128(a0 + kk * 32u);
+            const uint64_t bd = smem_desc_sw128(b0 + kk * 32u);
+            tc_mma_bf16(dt, ad, bd, idesc, (kb | kk) != 0u ? 1u : 0u);
+            if (X3) {
+              const uint64_t adl = smem_desc_sw128(a0 + KA_BYTES + KB_BYTES + kk * 32u);
+              const uint64_t bdl = smem_desc_sw128(a0 + 2 * KA_BYTES + KB_BYTES + kk * 32u);
+              tc_mma_bf16(dt, ad, bdl, idesc, 1u);
+              tc_mma_bf16(dt, adl, bd, idesc, 1u);
+            }
+          }
+          tc_commit(&ts->empty[s]);
+          issued = true;
+        }
+        if (!ok) break;
+        tc_commit(&ts->tfull[buf]);
+      }
+      if (issued) {
+        tc_commit(&ts->tdone);
+        volatile int no_abort = 0;
+        mbar_wait_bounded(&ts->tdone, 0, &no_abort, KWAIT_NS);
+      }
+    }
+  } else if (warp >= 4) {
+    const int q = warp & 3, set = (warp - 4) >> 2;
+    const uint32_t r = (uint32_t)q * 32u + (uint32_t)lane;
+    const uint32_t tbase = tmem_base + (((uint32_t)q * 32u) << 16) + (uint32_t)set * 256u;
+    uint64_t t = (uint64_t)set;
+    for (uint64_t tile = blockIdx.x + (uint64_t)set * gridDim.x; tile < ntiles;
+         tile += 2ull * gridDim.x, t += 2) {
+      const uint64_t mi = tile / nt, nj = tile % nt;
+      const uint64_t row = mi * KM_M + r, c0 = nj * KM_N;
+      const float ni = (row < n) ? xn2[row] : 0.0f;
+      // column norms only matter for the Gaussian kernel (broadcast loads)
+      auto colnorm = [&](uint64_t c) -> float {
+        return (f.kind == KM_KERNEL_GAUSSIAN && c < n) ? __ldg(xn2 + c) : 0.0f;
+      };
+      const bool okw = mbar_wait_bounded(&ts->tfull[set], (uint32_t)(t >> 1) & 1u, abort_flag, KWAIT_NS);
+      if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(4); break; }
+      tc_fence_after();
+      for (uint32_t pr = 0; pr < KM_N / 64; ++pr) {
+        uint32_t acc[64];
+        tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
+        tmem_ld_wait();
+        if (row < n) {
+          const uint64_t cb = c0 + pr * 64u;
+          if (OUT_BF16) {
+            __nv_bfloat16* Kr = reinterpret_cast<__nv_bfloat16*>(K) + row * n + cb;
+#pragma unroll
+            for (int j = 0; j < 64; j += 2) {
+              const float v0 = kfn_apply(f, __uint_as_float(acc[j]), ni, colnorm(cb + j));
+              const float v1 = kfn_apply(f, __uint_as_float(acc[j + 1]), ni, colnorm(cb + j + 1));
+              if (vec && cb + j + 1 < n) {
+                *reinterpret_cast<__nv_bfloat162*>(Kr + j) = __floats2bfloat162_rn(v0, v1);
+              } else {
+                if (cb + j < n) Kr[j] = __float2bfloat16_rn(v0);
+                if (cb + j + 1 < n) Kr[j + 1] = __float2bfloat16_rn(v1);
+              }
+              if (diag && cb + j == row) diag[row] = v0;
+              if (diag && cb + j + 1 == row) diag[row] = v1;
+            }
+          } else {
+            float* Kr = reinterpret_cast<float*>(K) + row * n + cb;
+#pragma unroll
+            for (int j = 0; j < 64; j += 4) {
+              float4 o;
+              o.x = kfn_apply(f, __uint_as_float(acc[j + 0]), ni, colnorm(cb + j + 0));
+              o.y = kfn_apply(f, __uint_as_float(acc[j + 1]), ni, colnorm(cb + j + 1));
+              o.z = kfn_apply(f, __uint_as_float(acc[j + 2]), ni, colnorm(cb + j + 2));
+              o.w = kfn_apply(f, __uint_as_float(acc[j + 3]), ni, colnorm(cb + j + 3));
+              if (vec && cb + j + 3 < n) {
+                *reinterpret_cast<float4*>(Kr + j) = o;
+              } else {
+                if (cb + j + 0 < n) Kr[j + 0] = o.x;
+                if (cb + j + 1 < n) Kr[j + 1] = o.y;
+                if (cb + j + 2 < n) Kr[j + 2] = o.z;
+                if (cb + j + 3 < n) Kr[j + 3] = o.w;
+              }
+              if (diag) {
+                if (cb + j + 0 == row) diag[row] = o.x;
+                if (cb + j + 1 == row) diag[row] = o.y;
+                if (cb + j + 2 == row) diag[row] = o.z;
+                if (cb + j + 3 == row) diag[row] = o.w;
+              }
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&ts->tempty[set]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 2) tmem_dealloc(tmem_base, 512);
+}
+
+// ---------------------------------------------------------------------------
+// (c) E = K V^T.  One warp per row of K at a time; the labels of all n points
+// sit in shared memory as bytes (k <= 256); every lane accumulates its columns
+// into private bins bins[c][lane] (no atomics, fixed order), then each lane
+// reduces two bins over the 32 lanes in lane order.  K rows are read once with
+// 16-byte (FP32) or 8-byte (BF16) loads.
+// ---------------------------------------------------------------------------
+template <bool KBF16>
+__global__ void __launch_bounds__(256)
+kkm_vk_kernel(const void* __restrict__ K, uint64_t n, uint32_t k, const uint32_t* __restrict__ labels,
+              float* __restrict__ E, DevState* st) {
+  if (st->done) return;
+  extern __shared__ __align__(16) uint8_t kk_smem[];
+  uint8_t* lab = kk_smem;                                            // n bytes
+  float* bins = reinterpret_cast<float*>(kk_smem + ((n + 15) & ~15ull));  // [8 warps][k][32]
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) lab[i] = (uint8_t)labels[i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* B = bins + (size_t)warp * k * 32;
+  for (uint32_t c = 0; c < k; ++c) B[c * 32 + lane] = 0.0f;
+  __syncwarp();
+  const uint64_t nw = (uint64_t)gridDim.x * 8;
+  for (uint64_t row = (uint64_t)blockIdx.x * 8 + warp; row < n; row += nw) {
+    // With n % 4 == 0 every row starts 16-byte (FP32) / 8-byte (BF16)
+    // aligned: lane l takes columns 4l..4l+3 of each 128-column stride.
+    // Otherwise one column per lane with plain loads.
+    const bool v4 = (n & 3) == 0;
+    if (KBF16) {
+      const __nv_bfloat16* Kr = reinterpret_cast<const __nv_bfloat16*>(K) + row * n;
+      if (v4) {
+        for (uint64_t j = (uint64_t)lane * 4; j < n; j += 128) {
+          const uint2 raw = __ldg(reinterpret_cast<const uint2*>(Kr + j));
+          const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw.x));
+          const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw.y));
+          const uint32_t l4 = *reinterpret_cast<const uint32_t*>(lab + j);
+          B[((l4 >> 0) & 255u) * 32 + lane] += a.x;
+          B[((l4 >> 8) & 255u) * 32 + lane] += a.y;
+          B[((l4 >> 16) & 255u) * 32 + lane] += b.x;
+          B[((l4 >> 24) & 255u) * 32 + lane] += b.y;
+        }
+      } else {
+        for (uint64_t j = lane; j < n; j += 32) B[lab[j] * 32 + lane] += __bfloat162float(Kr[j]);
+      }
+    } else {
+      const float* Kr = reinterpret_cast<const float*>(K) + row * n;
+      if (v4) {
+        for (uint64_t j = (uint64_t)lane * 4; j < n; j += 128) {
+          const float4 v = __ldg(reinterpret_cast<const float4*>(Kr + j));
+          const uint32_t l4 = *reinterpret_cast<const uint32_t*>(lab + j);
+          B[((l4 >> 0) & 255u) * 32 + lane] += v.x;
+          B[((l4 >> 8) & 255u) * 32 + lane] += v.y;
+          B[((l4 >> 16) & 255u) * 32 + lane] += v.z;
+          B[((l4 >> 24) & 255u) * 32 + lane] += v.w;
+        }
+      } else {
+        for (uint64_t j = lane; j < n; j += 32) B[lab[j] * 32 + lane] += Kr[j];
+      }
+    }
+    __syncwarp();
+    for (uint32_t c = lane; c < k; c += 32) {
+      float s = 0.0f;
+      for (int l = 0; l < 32; ++l) s += B[c * 32 + l];
+      E[row * k + c] = s;
+    }
+    __syncwarp();
+    for (uint32_t c = 0; c < k; ++c) B[c * 32 + lane] = 0.0f;
+    __syncwarp();
+  }
+}
+
+// ctilde_c = (1/|c|^2) sum_{i in c} E[i, c] in FP64, one warp per cluster over
+// its rows (label-sorted permutation), fixed reduction order.
+__global__ void kkm_ctilde_kernel(const float* __restrict__ E, uint32_t k, const uint32_t* __restrict__ perm,
+                                  const uint32_t* __restrict__ cstart, double* __restrict__ ct,
+                                  DevState* st) {
+  if (st->done) return;
+  const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= k) return;
+  const uint32_t s0 = cstart[c], s1 = cstart[c + 1];
+  double s = 0.0;
+  for (uint32_t p = s0 + lane; p < s1; p += 32) s += (double)E[(uint64_t)perm[p] * k + c];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    const double cnt = (double)(s1 - s0);
+    ct[c] = (s1 > s0) ? s / (cnt * cnt) : 0.0;
+  }
+}
+
+// D[i,c] = -2 E[i,c]/|c| + ctilde_c (ctilde == 0 -> +inf), argmin from
+// (0, FLT_MAX) with strict '<', new label and min; per-block FP64 score partials.
+__global__ void __launch_bounds__(256)
+kkm_dist_kernel(const float* __restrict__ E, uint64_t n, uint32_t k, const uint32_t* __restrict__ counts,
+                const double* __restrict__ ct, uint32_t* __restrict__ newlab,
+                double* __restrict__ part, DevState* st) {
+  if (st->done) return;
+  extern __shared__ float kd_smem[];
+  float* inv = kd_smem;            // -2/|c| (0 for empty clusters)
+  float* add = kd_smem + k;        // ctilde (+inf where 0)
+  for (uint32_t c = threadIdx.x; c < k; c += blockDim.x) {
+    const uint32_t cnt = counts[c];
+    inv[c] = cnt ? -2.0f / (float)cnt : 0.0f;
+    const float cf = (float)ct[c];
+    add[c] = (cf == 0.0f) ? __int_as_float(0x7f800000) : cf;
+  }
+  __syncthreads();
+  double acc = 0.0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const float* e = E + i * k;
+    float val = FLT_MAX;
+    uint32_t key = 0;
+    for (uint32_t c = 0; c < k; ++c) {
+      const float v = fmaf(inv[c], e[c], add[c]);
+      if (v < val) { val = v; key = c; }
+    }
+    newlab[i] = key;
+    acc += (double)val;
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// End of iteration: score (fixed-order sum of the block partials), the stop
+// rule, label hand-over.
+__global__ void kkm_control_kernel(const double* __restrict__ part, int np, LoopConsts lc,
+                                   int check, DevState* st) {
+  if (st->done) return;
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < np; ++i) s += part[i];
+    const uint32_t it = st->iter + 1;
+    st->iter = it;
+    st->score = s;
+    st->objective = s;
+    bool stop = false;
+    if (it >= lc.maxiter) stop = true;
+    else if (check && it > 1 && fabs(s - st->last_score) < (double)lc.tol) { st->converged_iter = it; stop = true; }
+    st->last_score = s;
+    if (stop) st->done = 1u;
+  }
+}
+
+__global__ void kkm_copy_labels_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
+                                       uint64_t n, DevState* st) {
+  // runs after the control kernel: the labels of the final iteration are
+  // copied too (the done flag is set by then), so only stop after copying.
+  if (st->iter == 0) return;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+}  // namespace km
+
+using namespace km;
 
 struct km_kkm {
   km_kkm_params p;
+  LloydEngine eng;          // sort machinery, stream, state (no Lloyd buffers used)
+  void* K = nullptr;        // n x n, float or bf16
+  float* diag = nullptr;
+  float* E = nullptr;       // n x k
+  double* ct = nullptr;
+  uint32_t* lab = nullptr;  // current labels
+  uint32_t* nlab = nullptr; // next labels
+  double* part = nullptr;
+  int dist_blocks = 0;
+  size_t vk_smem = 0;
+  bool ready = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int32_t* h_done = nullptr;
 };
+
+namespace km {
+namespace {
+
+KFn make_kfn(const km_kkm_params& p) {
+  KFn f;
+  f.kind = p.kernel_fn;
+  f.gamma = p.gamma;
+  f.coef = p.coef;
+  f.degree = p.degree;
+  f.inv2s2 = (p.sigma > 0) ? (float)(1.0 / (2.0 * (double)p.sigma * p.sigma)) : 0.0f;
+  return f;
+}
+
+km_status kfn_valid(int kind, int degree, float sigma) {
+  if (kind < KM_KERNEL_LINEAR || kind > KM_KERNEL_GAUSSIAN) return KM_ERR_ARG;
+  if (kind == KM_KERNEL_POLY && (degree < 1 || degree > 16)) return KM_ERR_ARG;
+  if (kind == KM_KERNEL_GAUSSIAN && !(sigma > 0)) return KM_ERR_ARG;
+  return KM_OK;
+}
+
+// Builds K (and diag) from points X (device, n x d) on stream s.  For the
+// tensor-core precisions it uses BF16 copies prepared by the engine.
+km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32_t d, const KFn& f,
+                              int precision, bool out_bf16, void* K, float* diag) {
+  cudaStream_t s = e.stream;
+  if (precision == KM_PREC_FP32) {
+    dim3 grid((unsigned)((n + 127) / 128), (unsigned)((n + 127) / 128));
+    if (out_bf16) kmat_f32_kernel<true><<<grid, 256, 0, s>>>(X, e.xn2, n, d, f, K, diag);
+    else kmat_f32_kernel<false><<<grid, 256, 0, s>>>(X, e.xn2, n, d, f, K, diag);
+    KM_CUDA_TRY(cudaGetLastError());
+    return KM_OK;
+  }
+  const bool x3 = precision == KM_PREC_BF16X3;
+  // Gaussian kernel: norms of the BF16 operands (see kmat_operand_norms_kernel);
+  // they overwrite xn2, which the kernel-matrix path does not otherwise use.
+  if (f.kind == KM_KERNEL_GAUSSIAN) {
+    kmat_operand_norms_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(e.Xb, x3 ? e.Xlo : nullptr, n,
+                                                                                e.dp, e.xn2);
+    KM_CUDA_TRY(cudaGetLastError());
+  }
+  CUtensorMap tA{}, tAlo{}, tB{}, tBlo{};
+  KM_TRY(encode_tmap_bf16(&tA, e.Xb, e.dp, n, 64, KM_M));
+  KM_TRY(encode_tmap_bf16(&tB, e.Xb, e.dp, n, 64, KM_N));
+  if (x3) {
+    KM_TRY(encode_tmap_bf16(&tAlo, e.Xlo, e.dp, n, 64, KM_M));
+    KM_TRY(encode_tmap_bf16(&tBlo, e.Xlo, e.dp, n, 64, KM_N));
+  } else {
+    tAlo = tA;
+    tBlo = tB;
+  }
+  const uint32_t KBn = e.dp / 64;
+  const size_t stage = (size_t)(KA_BYTES + KB_BYTES) * (x3 ? 2 : 1);
+  const size_t fixed = 1024 + sizeof(KmSmem) + 64;
+  size_t S = (227 * 1024 - fixed) / stage;
+  if (S > 8) S = 8;
+  if (S < 2) return KM_ERR_UNSUPPORTED;
+  const size_t smem = fixed + S * stage;
+  const uint64_t tiles = ((n + KM_M - 1) / KM_M) * ((n + KM_N - 1) / KM_N);
+  const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)e.num_sms);
+  const int vec = (n % 4 == 0) && (reinterpret_cast<uintptr_t>(K) % 16 == 0);
+#define KM_LAUNCH_KMAT(X3_, BF_)                                                                   \
+  do {                                                                                             \
+    KM_CUDA_TRY(cudaFuncSetAttribute(kmat_tc_kernel<X3_, BF_>,                                     \
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));     \
+    kmat_tc_kernel<X3_, BF_><<<grid, 384, smem, s>>>(tA, tAlo, tB, tBlo, e.xn2, n, KBn, (uint32_t)S, \
+                                                     f, K, diag, vec, e.st);                       \
+  } while (0)
+  if (x3) { if (out_bf16) KM_LAUNCH_KMAT(true, true); else KM_LAUNCH_KMAT(true, false); }
+  else { if (out_bf16) KM_LAUNCH_KMAT(false, true); else KM_LAUNCH_KMAT(false, false); }
+#undef KM_LAUNCH_KMAT
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
+
+km_status kkm_enqueue_iteration(km_kkm* h, const LoopConsts& lc) {
+  LloydEngine& e = h->eng;
+  const uint64_t n = h->p.n;
+  const uint32_t k = h->p.k;
+  cudaStream_t s = e.stream;
+  if (h->p.k_bf16)
+    kkm_vk_kernel<true><<<e.num_sms, 256, h->vk_smem, s>>>(h->K, n, k, h->lab, h->E, e.st);
+  else
+    kkm_vk_kernel<false><<<e.num_sms, 256, h->vk_smem, s>>>(h->K, n, k, h->lab, h->E, e.st);
+  KM_TRY(e.enqueue_sort(h->lab));
+  kkm_ctilde_kernel<<<(k * 32 + 255) / 256, 256, 0, s>>>(h->E, k, e.perm, e.cstart, h->ct, e.st);
+  kkm_dist_kernel<<<h->dist_blocks, 256, 2 * k * sizeof(float), s>>>(h->E, n, k, e.counts, h->ct, h->nlab,
+                                                                      h->part, e.st);
+  kkm_control_kernel<<<1, 32, 0, s>>>(h->part, h->dist_blocks, lc, h->p.check_converged, e.st);
+  kkm_copy_labels_kernel<<<(unsigned)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(h->nlab, h->lab, n, e.st);
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
+
+}  // namespace
+}  // namespace km
 
 extern "C" {
 
-km_status km_kernel_matrix(const float*, uint64_t, uint32_t, int32_t, float, float, int32_t, float,
-                           int32_t, int32_t, void*, float*, void*) {
-  return KM_ERR_UNSUPPORTED;
+km_status km_kernel_matrix(const float* X_dev, uint64_t n, uint32_t d, int32_t kernel_fn, float gamma,
+                           float coef, int32_t degree, float sigma, int32_t precision, int32_t out_bf16,
+                           void* K_dev, float* diag_dev, void* stream) {
+  if (!X_dev || !K_dev || n == 0 || d == 0) return KM_ERR_ARG;
+  KM_TRY(kfn_valid(kernel_fn, degree, sigma));
+  int dev;
+  if (cudaGetDevice(&dev) != cudaSuccess) { (void)cudaGetLastError(); return KM_ERR_NO_DEVICE; }
+  LloydEngine e;
+  KM_TRY(e.init(n, d, 1, precision, dev, stream, false));
+  KM_TRY(e.set_points(X_dev, true, false));
+  km_kkm_params p{};
+  p.kernel_fn = kernel_fn; p.gamma = gamma; p.coef = coef; p.degree = degree; p.sigma = sigma;
+  KM_TRY(build_kernel_matrix(e, X_dev, n, d, make_kfn(p), precision, out_bf16 != 0, K_dev, diag_dev));
+  return e.check_device_error();
 }
 
 km_status km_kkm_create(const km_kkm_params* p, km_kkm** out) {
   if (!p || !out) return KM_ERR_ARG;
   *out = nullptr;
-  return KM_ERR_UNSUPPORTED;
+  if (p->n == 0 || p->d == 0 || p->k == 0 || p->k > p->n || p->maxiter == 0) return KM_ERR_ARG;
+  if (p->k > 256) return KM_ERR_UNSUPPORTED;   // byte labels in shared memory
+  if (!(p->tol >= 0.0f)) return KM_ERR_ARG;
+  KM_TRY(kfn_valid(p->kernel_fn, p->degree, p->sigma));
+  const uint64_t nn = p->n * p->n;
+  if (nn / p->n != p->n) return KM_ERR_ARG;
+  const size_t vk_smem = ((p->n + 15) & ~15ull) + (size_t)8 * p->k * 32 * sizeof(float);
+  if (vk_smem > 227 * 1024) return KM_ERR_UNSUPPORTED;
+  km_kkm* h = new (std::nothrow) km_kkm();
+  if (!h) return KM_ERR_ALLOC;
+  h->p = *p;
+  h->vk_smem = vk_smem;
+  km_status s = h->eng.init(p->n, p->d, p->k, p->precision, p->device, p->stream, true);
+  auto fail = [&](km_status st) { km_kkm_destroy(h); return st; };
+  if (s != KM_OK) return fail(s);
+  const size_t kbytes = nn * (p->k_bf16 ? 2 : 4);
+  if (cudaMalloc(&h->K, kbytes) != cudaSuccess || cudaMalloc(&h->diag, sizeof(float) * p->n) != cudaSuccess ||
+      cudaMalloc(&h->E, sizeof(float) * p->n * p->k) != cudaSuccess ||
+      cudaMalloc(&h->ct, sizeof(double) * p->k) != cudaSuccess ||
+      cudaMalloc(&h->lab, sizeof(uint32_t) * p->n) != cudaSuccess ||
+      cudaMalloc(&h->nlab, sizeof(uint32_t) * p->n) != cudaSuccess ||
+      cudaMalloc(&h->part, sizeof(double) * 1024) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(KM_ERR_ALLOC);
+  }
+  h->dist_blocks = (int)std::min<uint64_t>((p->n + 255) / 256, 1024);
+  if (cudaFuncSetAttribute(kkm_vk_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vk_smem) != cudaSuccess ||
+      cudaFuncSetAttribute(kkm_vk_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vk_smem) != cudaSuccess ||
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess ||
+      cudaMallocHost(reinterpret_cast<void**>(&h->h_done), sizeof(int32_t)) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(KM_ERR_CUDA);
+  }
+  *out = h;
+  return KM_OK;
 }
 
-km_status km_kkm_set_data(km_kkm* h, const float* X, int) {
+km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device) {
   if (!h || !X) return KM_ERR_ARG;
-  return KM_ERR_UNSUPPORTED;
+  LloydEngine& e = h->eng;
+  KM_TRY(e.set_points(X, on_device != 0, true));
+  KM_TRY(build_kernel_matrix(e, e.X, h->p.n, h->p.d, make_kfn(h->p), h->p.precision, h->p.k_bf16 != 0,
+                             h->K, h->diag));
+  KM_TRY(e.check_device_error());
+  h->ready = true;
+  return KM_OK;
 }
 
-km_status km_kkm_fit(km_kkm* h, const uint32_t*, uint32_t*, km_result*) {
+km_status km_kkm_fit(km_kkm* h, const uint32_t* init_labels, uint32_t* labels_out, km_result* res) {
   if (!h) return KM_ERR_ARG;
-  return KM_ERR_UNSUPPORTED;
+  if (!h->ready) return KM_ERR_STATE;
+  LloydEngine& e = h->eng;
+  KM_CUDA_TRY(cudaSetDevice(e.device));
+  KM_TRY(e.reset_state());
+  const uint64_t n = h->p.n;
+  if (init_labels) {
+    for (uint64_t i = 0; i < n; ++i)
+      if (init_labels[i] >= h->p.k) return KM_ERR_ARG;
+    KM_CUDA_TRY(cudaMemcpyAsync(h->lab, init_labels, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, e.stream));
+  } else {
+    round_robin_labels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, e.stream>>>(h->lab, n, h->p.k);
+    KM_CUDA_TRY(cudaGetLastError());
+  }
+  LoopConsts lc{h->p.maxiter, h->p.tol, h->p.check_converged ? KM_CONV_SCORE : KM_CONV_NONE};
+  KM_CUDA_TRY(cudaEventRecord(h->ev0, e.stream));
+  uint64_t launched = 0, batch = h->p.check_converged ? 4 : h->p.maxiter;
+  while (launched < h->p.maxiter) {
+    const uint64_t target = std::min<uint64_t>(h->p.maxiter, launched + batch);
+    for (; launched < target; ++launched) KM_TRY(kkm_enqueue_iteration(h, lc));
+    if (launched >= h->p.maxiter) break;
+    KM_CUDA_TRY(cudaMemcpyAsync(h->h_done, &e.st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, e.stream));
+    KM_CUDA_TRY(cudaStreamSynchronize(e.stream));
+    if (*h->h_done) break;
+    batch = std::min<uint64_t>(batch * 2, 64);
+  }
+  KM_CUDA_TRY(cudaEventRecord(h->ev1, e.stream));
+  KM_TRY(e.check_device_error());
+  float ms = 0;
+  KM_CUDA_TRY(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  if (labels_out)
+    KM_CUDA_TRY(cudaMemcpyAsync(labels_out, h->lab, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, e.stream));
+  KM_CUDA_TRY(cudaStreamSynchronize(e.stream));
+  const DevState& s = *e.h_st;
+  if (res) {
+    std::memset(res, 0, sizeof(*res));
+    res->iterations = s.iter;
+    res->converged = s.converged_iter != 0;
+    res->converged_iter = s.converged_iter ? s.converged_iter : h->p.maxiter;
+    res->objective = s.objective;
+    res->score = s.score;
+    res->fit_ms = ms;
+  }
+  return KM_OK;
 }
 
-void km_kkm_destroy(km_kkm* h) { delete h; }
+void km_kkm_destroy(km_kkm* h) {
+  if (!h) return;
+  if (h->eng.device >= 0) cudaSetDevice(h->eng.device);
+  if (h->K) cudaFree(h->K);
+  if (h->diag) cudaFree(h->diag);
+  if (h->E) cudaFree(h->E);
+  if (h->ct) cudaFree(h->ct);
+  if (h->lab) cudaFree(h->lab);
+  if (h->nlab) cudaFree(h->nlab);
+  if (h->part) cudaFree(h->part);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->h_done) cudaFreeHost(h->h_done);
+  delete h;
+}
 
 }  // extern "C"

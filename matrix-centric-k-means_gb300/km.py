@@ -179,6 +179,58 @@ class Lloyd:
             pass
 
 
+def kernel_matrix(X, kernel="linear", gamma=1.0, coef=1.0, degree=2, sigma=1.0, precision="fp32",
+                  out_bf16=False, want_diag=False):
+    """K = f(X X^T) for a torch CUDA tensor X (n, d)."""
+    import torch
+    n, d = X.shape
+    K = torch.empty((n, n), dtype=torch.bfloat16 if out_bf16 else torch.float32, device=X.device)
+    dg = torch.empty(n, dtype=torch.float32, device=X.device) if want_diag else None
+    check(_lib().km_kernel_matrix(_ptr(X), n, d, KERNEL[kernel], gamma, coef, degree, sigma, PREC[precision],
+                                  int(out_bf16), _ptr(K), _ptr(dg), torch.cuda.current_stream().cuda_stream),
+          "km_kernel_matrix")
+    return (K, dg) if want_diag else K
+
+
+class KernelKMeans:
+    """Handle over km_kkm_*: kernel k-means with the reference GPU path's semantics."""
+
+    def __init__(self, n, d, k, kernel="linear", gamma=1.0, coef=1.0, degree=2, sigma=1.0, tol=1e-4,
+                 maxiter=30, precision="fp32", k_bf16=False, check_converged=False, device=0, stream=0):
+        self.p = KkmParams(n, d, k, tol, maxiter, KERNEL[kernel], gamma, coef, sigma, degree, PREC[precision],
+                           int(k_bf16), int(check_converged), device, stream or None)
+        h = C.c_void_p()
+        check(_lib().km_kkm_create(C.byref(self.p), C.byref(h)), "km_kkm_create")
+        self.h = h
+
+    def set_data(self, X):
+        if isinstance(X, np.ndarray):
+            X = np.ascontiguousarray(X, dtype=np.float32)
+            check(_lib().km_kkm_set_data(self.h, X.ctypes.data, 0), "km_kkm_set_data")
+        else:
+            check(_lib().km_kkm_set_data(self.h, X.data_ptr(), 1), "km_kkm_set_data")
+        return self
+
+    def fit(self, init_labels=None):
+        lab = np.empty(self.p.n, np.uint32)
+        il = None if init_labels is None else np.ascontiguousarray(init_labels, np.uint32)
+        r = Result()
+        check(_lib().km_kkm_fit(self.h, None if il is None else il.ctypes.data, lab.ctypes.data, C.byref(r)),
+              "km_kkm_fit")
+        return lab, r
+
+    def close(self):
+        if self.h:
+            _lib().km_kkm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def assign(X, Cc, precision="fp32", want_mindist=False):
     """labels (and fast-path min distance) of torch CUDA tensors X (n,d), C (k,d)."""
     import torch

@@ -1,0 +1,114 @@
+"""GPU parity of kernel k-means (the reference's popcorn GPU path) through the C
+ABI: the kernel matrix K = f(X X^T) against an FP64 torch reference, and the
+iteration against the FP64 oracle (orc_kernel_kmeans, itself checked against
+an independent numpy statement in test_oracle.py)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import helpers
+
+pytestmark = pytest.mark.gpu
+
+KERNELS = [("linear", dict()), ("polynomial", dict(gamma=1 / 16, coef=1.0, degree=2)),
+           ("sigmoid", dict(gamma=0.01, coef=1.0)), ("gaussian", dict(sigma=3.0))]
+# relative tolerance of K against FP64, as a fraction of the scale max|K| (or of
+# |gamma| ||x|| ||y|| for the argument of f)
+TOL = {"fp32": 2e-5, "bf16x3": 2e-4, "bf16": 3e-2}
+
+
+def ref_kernel(X, kind, p):
+    Xd = X.double()
+    G = Xd @ Xd.T
+    sq = (Xd * Xd).sum(1)
+    if kind == "linear":
+        return G
+    if kind == "polynomial":
+        return (p["gamma"] * G + p["coef"]) ** p["degree"]
+    if kind == "sigmoid":
+        return (p["gamma"] * G + p["coef"]).tanh()
+    return (-(sq[:, None] + sq[None] - 2 * G).clamp_min(0) / (2 * p["sigma"] ** 2)).exp()
+
+
+@pytest.mark.parametrize("out_bf16", [False, True])
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "bf16x3"])
+@pytest.mark.parametrize("kind,params", KERNELS, ids=[k for k, _ in KERNELS])
+@pytest.mark.parametrize("shape", [(1000, 37), (2048, 128)])
+def test_kernel_matrix_vs_fp64(km, gpu, kind, params, prec, out_bf16, shape):
+    import torch
+    n, d = shape
+    X = torch.from_numpy(helpers.synth_blobs_np(n, d, 5, -1, 1, 0.5, 3)[0]).to(gpu)
+    K, dg = km.kernel_matrix(X, kernel=kind, precision=prec, out_bf16=out_bf16, want_diag=True, **params)
+    ref = ref_kernel(X, kind, params)
+    scale = float(ref.abs().max())
+    tol = TOL[prec] + (2 ** -8 if out_bf16 else 0.0)
+    err = float((K.double() - ref).abs().max())
+    assert err <= tol * scale * 4, (err, scale)
+    np.testing.assert_allclose(torch.diagonal(K).double().cpu().numpy(), dg.double().cpu().numpy(),
+                               rtol=2 ** -8 if out_bf16 else 0, atol=0)
+
+
+def oracle_kkm(X, kind, params, k, maxiter, tol, check):
+    X = np.ascontiguousarray(X, np.float32)
+    n, d = X.shape
+    Kd = np.empty((n, n))
+    kid = {"linear": 0, "polynomial": 1, "sigmoid": 2, "gaussian": 3}[kind]
+    helpers.oracle().orc_kernel_matrix(X.ctypes.data, n, d, kid, params.get("gamma", 1.0), params.get("coef", 1.0),
+                                       params.get("degree", 2), params.get("sigma", 1.0), 8, Kd.ctypes.data)
+    lab = (np.arange(n) % k).astype(np.uint32)
+    sc = C.c_double(0)
+    ex = C.c_uint64(0)
+    it = helpers.oracle().orc_kernel_kmeans(Kd.ctypes.data, n, k, maxiter, tol, int(check), 8, lab.ctypes.data,
+                                            C.byref(sc), C.byref(ex))
+    return it, lab, sc.value, ex.value
+
+
+def test_kkm_linear_integer_data_exact(km, gpu):
+    """Integer-valued points and the linear kernel: K, E and the distances are
+    exact in every precision, so labels and iteration count equal the oracle's."""
+    X, _ = helpers.synth_blobs_np(1500, 16, 7, 0, 8, 2.0, 5, round_clip=True)
+    it_o, lab_o, sc_o, ex_o = oracle_kkm(X, "linear", {}, 7, 40, 1e-9, True)
+    for prec in ("fp32", "bf16", "bf16x3"):
+        m = km.KernelKMeans(1500, 16, 7, kernel="linear", maxiter=40, tol=1e-9, precision=prec,
+                            check_converged=True).set_data(X)
+        lab, r = m.fit()
+        m.close()
+        np.testing.assert_array_equal(lab, lab_o)
+        assert r.converged_iter == it_o
+        assert abs(r.score - sc_o) <= 1e-6 * max(1.0, abs(sc_o))
+
+
+@pytest.mark.parametrize("kb16", [False, True])
+@pytest.mark.parametrize("prec", ["fp32", "bf16x3", "bf16"])
+@pytest.mark.parametrize("kind,params", [("polynomial", dict(gamma=1 / 32, coef=1.0, degree=2)),
+                                         ("gaussian", dict(sigma=2.0))])
+def test_kkm_vs_fp64_oracle(km, gpu, kind, params, prec, kb16):
+    X, _ = helpers.synth_blobs_np(3000, 32, 6, -1, 1, 0.35, 9)
+    maxiter = 8
+    it_o, lab_o, sc_o, _ = oracle_kkm(X, kind, params, 6, maxiter, 0.0, False)
+    m = km.KernelKMeans(3000, 32, 6, kernel=kind, maxiter=maxiter, precision=prec, k_bf16=kb16,
+                        **params).set_data(X)
+    lab, r = m.fit()
+    m.close()
+    agree = float((lab == lab_o).mean())
+    reduced = prec == "bf16" or kb16
+    # K stored in BF16 keeps 8 significant bits of every K_ij; with the
+    # Gaussian kernel the cluster margins of E are thin and 8 iterations let a
+    # few per cent of the labels drift from the FP64 trajectory.
+    floor = 0.999 if not reduced else (0.98 if kind == "gaussian" else 0.99)
+    assert agree >= floor, agree
+    rel = abs(r.score - sc_o) / abs(sc_o)
+    assert rel <= (1e-5 if prec == "fp32" and not kb16 else 1e-3 if not reduced else 2e-2), rel
+    assert r.iterations == maxiter
+
+
+def test_kkm_given_initial_labels_and_bad_labels(km, gpu):
+    X, _ = helpers.synth_blobs_np(500, 8, 4, -2, 2, 0.5, 1)
+    m = km.KernelKMeans(500, 8, 4, kernel="linear", maxiter=5).set_data(X)
+    lab, r = m.fit(init_labels=np.zeros(500, np.uint32) + (np.arange(500) % 2))
+    assert lab.max() < 4
+    with pytest.raises(km.KmError) as e:
+        m.fit(init_labels=np.full(500, 9, np.uint32))
+    assert e.value.status == km.KM_ERR_ARG
+    m.close()
