@@ -40,7 +40,6 @@ N, D, K = 1_048_576, 128, 256
 BLOBS, LO, HI, SIGMA, DATA_SEED = 256, -10.0, 10.0, 1.0, 1000
 KM_SEED, TOL = 0, 1e-4
 METRIC = "iters/s (n=1M,d=128,k=256): BF16-TC vs FP32 plain at equal labels; % of peak"
-LAUNCHES_PER_ITER = 9
 
 
 def peaks():
@@ -102,31 +101,43 @@ class Clocks:
                 "samples": len(self.rows)}
 
 
+def bench_config(world):
+    """The `config` object both arms print."""
+    return {"workload": f"lloyd n={N} d={D} k={K} (256 gaussian blobs, sigma 1, centers U[-10,10])",
+            "n": N, "d": D, "k": K, "maxiter": "steps (stop rule off)",
+            "l2": "inputs larger than L2 (X fp32 512 MiB, bf16 256 MiB; L2 129 MB)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def make_data(km):
     return km.synth_blobs(N, D, BLOBS, LO, HI, SIGMA, DATA_SEED, nthreads=os.cpu_count() or 8)
 
 
-def run_cpu_sample(threads, sample_rows, reps=1, use_ref=False):
-    """The reference CPU k-means iteration (kmeans.cpp:86-148) on a bounded
-    sample: one assignment + update of `sample_rows` points against k=256
-    centroids on `threads` host threads (the oracle port), or the reference's own
-    build where it exists; scaled to iterations/s of the full n."""
+def run_cpu_sample(X, threads, sample_rows, min_seconds, use_ref=False):
+    """The reference CPU k-means iteration (comparisons/CPU_Kmeans/src/kmeans.cpp:86-155:
+    assignment by the CPU distance formula, strict-< argmin, sum-then-scale
+    update) on the first `sample_rows` points of the workload against k seeded
+    sample centroids, repeated until `min_seconds` have passed; on `threads`
+    host threads (the oracle port), or the reference's own single-threaded build
+    where it exists.  Returns full-n iterations/s (scaled by n/sample_rows when
+    the sample is smaller than n), the seconds of one repetition, and the
+    repetitions run."""
     import helpers
-    km = helpers.km()
-    X = km.synth_blobs(sample_rows, D, BLOBS, LO, HI, SIGMA, DATA_SEED, nthreads=threads)
+    Xs = np.ascontiguousarray(X[:sample_rows])
     rng = np.random.default_rng(0)
-    C0 = X[rng.choice(sample_rows, K, replace=False)].copy()
+    C0 = Xs[rng.choice(sample_rows, K, replace=False)].copy()
     t = []
-    for _ in range(reps):
+    t_start = time.perf_counter()
+    while not t or (time.perf_counter() - t_start < min_seconds and len(t) < 64):
         t0 = time.perf_counter()
         if use_ref:
-            helpers.ref_lloyd(X, K, -1.0, KM_SEED, 1)
+            helpers.ref_lloyd(Xs, K, -1.0, KM_SEED, 1)
         else:
-            lab, _ = helpers.orc_assign(X, C0, threads=threads)
-            helpers.orc_update(X, lab, K, threads=threads)
+            lab, _ = helpers.orc_assign(Xs, C0, threads=threads)
+            helpers.orc_update(Xs, lab, K, threads=threads)
         t.append(time.perf_counter() - t0)
-    per_iter_full = min(t) * (N / sample_rows)
-    return 1.0 / per_iter_full, min(t)
+    per_iter_full = statistics.median(t) * (N / sample_rows)
+    return 1.0 / per_iter_full, statistics.median(t), len(t)
 
 
 def reference_arm(args, rank):
@@ -137,23 +148,29 @@ def reference_arm(args, rank):
     use_ref = helpers.reference_lib() is not None
     if use_ref:
         threads = 1                           # the reference CPU k-means is single-threaded
-    sample = 4096 if not use_ref else 2048
+    # the port runs one whole iteration over all n points per step; the
+    # single-threaded reference build (about 30 s per full iteration) a 1/16 slice
+    sample = N if not use_ref else N // 16
+    X = make_data(helpers.km())
     vals = []
     for i in range(args.warmup + args.steps):
-        v, secs = run_cpu_sample(threads, sample, 1, use_ref)
+        v, secs, _ = run_cpu_sample(X, threads, sample, 0.0, use_ref)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
     kind = "reference" if use_ref else "port"
+    what = ("the reference's comparisons/CPU_Kmeans built from its sources (oracle/_ref)" if use_ref else
+            "the oracle port of comparisons/CPU_Kmeans/src/kmeans.cpp:86-155")
     line = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": f"lloyd n={N} d={D} k={K} (256 gaussian blobs)", "n": N, "d": D, "k": K},
+        "config": bench_config(args.gpus),
         "cpu_baseline": {"value": value, "unit": "iters/s", "cores": threads, "kind": kind,
-                         "sample": f"one assignment+update of {sample} of the {N} points against k={K}"
-                                   f" centroids per step, scaled by n/{sample}"},
+                         "sample": f"{what}: one assignment+update of {sample} of the {N} points against "
+                                   f"k={K} centroids per step on {threads} host threads"
+                                   + (f", scaled by n/{sample}" if sample != N else "")},
         "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     return line
@@ -197,7 +214,8 @@ def ours_arm(args, rank, world):
             # the fit above includes the seeded init; the library's own loop timer
             # brackets exactly the `steps` iterations
             timing[prec] = dict(ms_total=ms, ms_loop=r.fit_ms, iters=r.iterations, clocks=clk.summary(),
-                                refined=r.refined_rows, full=r.full_rescore_rows, objective=r.objective)
+                                refined=r.refined_rows, full=r.full_rescore_rows, objective=r.objective,
+                                launches=r.kernel_launches)
             labels[prec] = lab
             res[prec] = m
     ms_loop = timing[args.precision]["ms_loop"]
@@ -269,20 +287,19 @@ def ours_arm(args, rank, world):
     cpu = None
     if rank == 0:
         threads = os.cpu_count() or 1
-        v, secs = run_cpu_sample(threads, 8192, 2)
+        v, secs, reps = run_cpu_sample(X, threads, N, 10.0)
         cpu = {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
-               "sample": f"one assignment+update (oracle port of comparisons/CPU_Kmeans kmeans.cpp:86-148) "
-                         f"of 8192 of the {N} points against k={K}, {secs:.2f} s, scaled by n/8192"}
+               "sample": f"whole iterations (assignment+update, oracle port of comparisons/CPU_Kmeans/src/"
+                         f"kmeans.cpp:86-155) over all {N} points against k={K}: {reps} repetitions of "
+                         f"{secs:.2f} s each, median"}
     clocks = timing[args.precision]["clocks"]
     line = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_loop / iters, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if args.precision != "fp32" else "f32",
         "data": "synthetic",
-        "config": {"workload": f"lloyd n={N} d={D} k={K} (256 gaussian blobs, sigma 1, centers U[-10,10])",
-                   "n": N, "d": D, "k": K, "precision": args.precision,
-                   "l2": "inputs larger than L2 (X fp32 512 MiB, bf16 256 MiB; L2 129 MB)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": bench_config(world),
+        "precision": args.precision,
         "fp32_plain": {"value": fp32_ips, "unit": "iters/s", "stages_ms": stages32},
         "speedup_vs_fp32_plain": value / world / fp32_ips,
         "label_agreement_vs_fp32": agree,
@@ -296,14 +313,24 @@ def ours_arm(args, rank, world):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "clocks": clocks,
-        "gpu_launches": LAUNCHES_PER_ITER * iters,
+        "gpu_launches": timing[args.precision]["launches"],
     }
     return line
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum per launch from the committed ncu
-# summaries (profiles/); None until captured.
-TRAFFIC = {}
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the stage's
+# dominant kernel, from one ncu capture of this command
+# (profiles/lloyd_iteration_n1M_d128_k256_launches.md; averages over the
+# launches of each arm).  Keys: (precision, stage).
+TRAFFIC = {
+    ("bf16", "distance+argmin"): 282.6e6,        # assign_tc_kernel<0>
+    ("bf16", "refine"): 136.5e6 + 6.6e6,         # refine_cands_kernel + refine_full_kernel
+    ("bf16", "label sort"): 10.6e6,              # seg_hist + seg_scan + cluster_scan + seg_scatter
+    ("bf16", "centroid sums"): 541.8e6,          # update_sums_bulk_kernel
+    ("bf16", "finalize+control"): 0.7e6,
+    ("fp32", "distance+argmin"): 549.2e6,        # assign_f32_kernel<1>
+    ("fp32", "centroid sums"): 541.9e6,
+}
 
 
 def main():

@@ -85,6 +85,15 @@ typedef enum km_kernel_fn {
   KM_KERNEL_GAUSSIAN = 3
 } km_kernel_fn;
 
+/* Empty clusters.  ZERO: the centroid of an empty cluster is the zero vector
+ * and stays selectable (reference CPU rule, comparisons/CPU_Kmeans/src/kmeans.cpp:131-155).
+ * EXCLUDE: an empty cluster's distance is +inf from then on, so it is never
+ * chosen again (reference GPU rule: c~ = 0 -> +inf, src/kernels/distances.cu:588-599). */
+typedef enum km_empty {
+  KM_EMPTY_ZERO = 0,
+  KM_EMPTY_EXCLUDE = 1
+} km_empty;
+
 typedef struct km_lloyd_params {
   uint64_t n;          /* points */
   uint32_t d;          /* dimensions */
@@ -97,6 +106,7 @@ typedef struct km_lloyd_params {
   int32_t conv;        /* km_conv */
   int32_t device;      /* CUDA device ordinal */
   void* stream;        /* cudaStream_t, or NULL */
+  int32_t empty;       /* km_empty */
 } km_lloyd_params;
 
 typedef struct km_result {
@@ -110,6 +120,7 @@ typedef struct km_result {
   uint64_t refined_rows;    /* rows re-scored with the CPU formula, all iterations */
   uint64_t full_rescore_rows; /* of those, rows re-scored against all k centroids */
   double fit_ms;            /* device time of the iteration loop */
+  uint64_t kernel_launches; /* kernels this library launched inside the timed iteration loop */
 } km_result;
 
 typedef struct km_lloyd km_lloyd;
@@ -120,6 +131,10 @@ const char* km_version(void);
 
 /* Number of sm_103 devices visible; 0 when none. */
 int km_device_count(void);
+
+/* Free and total device memory of `device` (the reference prints the footprint
+ * from cudaMemGetInfo, src/kmeans.cu:1090-1096). */
+km_status km_mem_info(int32_t device, uint64_t* free_bytes, uint64_t* total_bytes);
 
 /* ---- Lloyd k-means handle: replaces Kmeans(...) + run() + get_score() ---- */
 
@@ -136,6 +151,11 @@ km_status km_lloyd_set_data(km_lloyd* h, const float* X, int on_device);
  * (may be NULL); res may be NULL. */
 km_status km_lloyd_fit(km_lloyd* h, const float* C0, uint32_t* labels_out,
                        float* centroids_out, km_result* res);
+
+/* Changes the iteration budget and stop rule of a handle before its next fit
+ * (Kmeans::run(maxiter, check_converged) sets both at run time,
+ * src/kmeans.cuh:130). */
+km_status km_lloyd_configure(km_lloyd* h, uint64_t maxiter, float tol, int32_t conv);
 
 /* Device-resident results of the last fit (valid until the next fit/destroy). */
 km_status km_lloyd_device_results(km_lloyd* h, const uint32_t** labels_dev,
@@ -228,6 +248,8 @@ typedef struct km_kkm_params {
 km_status km_kkm_create(const km_kkm_params* p, km_kkm** out);
 /* Builds K from n*d points (host or device). */
 km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device);
+/* Changes maxiter, tol and the -c stop rule before the next fit. */
+km_status km_kkm_configure(km_kkm* h, uint64_t maxiter, float tol, int32_t check_converged);
 /* init_labels: n host labels, or NULL for the reference's i % k. */
 km_status km_kkm_fit(km_kkm* h, const uint32_t* init_labels, uint32_t* labels_out, km_result* res);
 void km_kkm_destroy(km_kkm* h);

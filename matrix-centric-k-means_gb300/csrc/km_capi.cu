@@ -39,6 +39,19 @@ __global__ void round_robin_labels_kernel(uint32_t* labels, uint64_t n, uint32_t
 
 namespace {
 
+uint64_t count_kernel_nodes(cudaGraph_t g) {
+  size_t nn = 0;
+  if (cudaGraphGetNodes(g, nullptr, &nn) != cudaSuccess) { (void)cudaGetLastError(); return 0; }
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn && cudaGraphGetNodes(g, nodes.data(), &nn) != cudaSuccess) { (void)cudaGetLastError(); return 0; }
+  uint64_t c = 0;
+  for (cudaGraphNode_t v : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(v, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++c;
+  }
+  return c;
+}
+
 // Seeded sample picks exactly as the reference CPU k-means draws them
 // (comparisons/CPU_Kmeans/src/kmeans.cpp:22-29, :49-84): mt19937(seed_seq{seed}),
 // uniform_int_distribution<int>(0, n-1), points equal by value to an earlier
@@ -127,6 +140,7 @@ struct km_lloyd {
   cudaGraphExec_t graph = nullptr;
   LoopConsts graph_lc{};
   int graph_iters = 0;
+  uint64_t graph_kernels = 0;     // kernel nodes in one replay of `graph`
   int32_t* h_done = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
@@ -165,6 +179,7 @@ km_status km_lloyd_create(const km_lloyd_params* p, km_lloyd** out) {
   *out = nullptr;
   if (p->init < KM_INIT_SAMPLE || p->init > KM_INIT_GIVEN) return KM_ERR_ARG;
   if (p->conv < KM_CONV_SHIFT || p->conv > KM_CONV_NONE) return KM_ERR_ARG;
+  if (p->empty != KM_EMPTY_ZERO && p->empty != KM_EMPTY_EXCLUDE) return KM_ERR_ARG;
   if (!(p->tol >= 0.0f) || p->maxiter == 0) return KM_ERR_ARG;
   km_lloyd* h = new (std::nothrow) km_lloyd();
   if (!h) return KM_ERR_ALLOC;
@@ -174,6 +189,25 @@ km_status km_lloyd_create(const km_lloyd_params* p, km_lloyd** out) {
   if (s == KM_OK && (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)) s = KM_ERR_CUDA;
   if (s != KM_OK) { km_lloyd_destroy(h); return s; }
   *out = h;
+  return KM_OK;
+}
+
+km_status km_mem_info(int32_t device, uint64_t* free_bytes, uint64_t* total_bytes) {
+  if (!free_bytes || !total_bytes) return KM_ERR_ARG;
+  if (km_device_count() == 0) return KM_ERR_NO_DEVICE;
+  KM_CUDA_TRY(cudaSetDevice(device));
+  size_t f = 0, t = 0;
+  KM_CUDA_TRY(cudaMemGetInfo(&f, &t));
+  *free_bytes = f;
+  *total_bytes = t;
+  return KM_OK;
+}
+
+km_status km_lloyd_configure(km_lloyd* h, uint64_t maxiter, float tol, int32_t conv) {
+  if (!h || maxiter == 0 || !(tol >= 0.0f) || conv < KM_CONV_SHIFT || conv > KM_CONV_NONE) return KM_ERR_ARG;
+  h->p.maxiter = maxiter;
+  h->p.tol = tol;
+  h->p.conv = conv;
   return KM_OK;
 }
 
@@ -200,11 +234,11 @@ km_status km_lloyd_fit(km_lloyd* h, const float* C0, uint32_t* labels_out, float
   }
   KM_TRY(e.set_centroids_dev(e.C));
 
-  LoopConsts lc{h->p.maxiter, h->p.tol, h->p.conv};
+  LoopConsts lc{h->p.maxiter, h->p.tol, h->p.conv, h->p.empty};
   // One captured graph = G iterations; relaunched until the device says done.
   const int G = (int)std::min<uint64_t>(h->p.maxiter, h->p.conv == KM_CONV_NONE ? 8 : 2);
   if (!h->graph || h->graph_iters != G || h->graph_lc.maxiter != lc.maxiter ||
-      h->graph_lc.tol != lc.tol || h->graph_lc.conv != lc.conv) {
+      h->graph_lc.tol != lc.tol || h->graph_lc.conv != lc.conv || h->graph_lc.empty != lc.empty) {
     if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     cudaGraph_t g = nullptr;
     KM_CUDA_TRY(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
@@ -213,6 +247,7 @@ km_status km_lloyd_fit(km_lloyd* h, const float* C0, uint32_t* labels_out, float
     cudaError_t ce = cudaStreamEndCapture(e.stream, &g);
     if (cs != KM_OK) { if (g) cudaGraphDestroy(g); return cs; }
     KM_CUDA_TRY(ce);
+    h->graph_kernels = count_kernel_nodes(g);
     cudaError_t ie = cudaGraphInstantiate(&h->graph, g, 0);
     cudaGraphDestroy(g);
     KM_CUDA_TRY(ie);
@@ -220,13 +255,14 @@ km_status km_lloyd_fit(km_lloyd* h, const float* C0, uint32_t* labels_out, float
     h->graph_iters = G;
   }
   KM_CUDA_TRY(cudaEventRecord(h->ev0, e.stream));
-  uint64_t launched = 0;
+  uint64_t launched = 0, replays = 0;
   uint64_t batch = (h->p.conv == KM_CONV_NONE) ? h->p.maxiter : 4;
   while (launched < h->p.maxiter) {
     const uint64_t target = std::min<uint64_t>(h->p.maxiter, launched + batch);
     while (launched < target) {
       KM_CUDA_TRY(cudaGraphLaunch(h->graph, e.stream));
       launched += (uint64_t)G;
+      ++replays;
     }
     if (launched >= h->p.maxiter) break;
     KM_CUDA_TRY(cudaMemcpyAsync(h->h_done, &e.st->done, sizeof(int32_t), cudaMemcpyDeviceToHost, e.stream));
@@ -255,6 +291,7 @@ km_status km_lloyd_fit(km_lloyd* h, const float* C0, uint32_t* labels_out, float
     res->refined_rows = s.refined_total;
     res->full_rescore_rows = s.full_total;
     res->fit_ms = ms;
+    res->kernel_launches = replays * h->graph_kernels;
   }
   return KM_OK;
 }
@@ -278,7 +315,7 @@ km_status km_lloyd_profile(km_lloyd* h, uint64_t iters, double* stage_ms) {
   e.h_st->done = 0;
   e.h_st->iter = 0;
   KM_CUDA_TRY(cudaMemcpyAsync(e.st, e.h_st, sizeof(DevState), cudaMemcpyHostToDevice, e.stream));
-  LoopConsts lc{~0ull, h->p.tol, KM_CONV_NONE};
+  LoopConsts lc{~0ull, h->p.tol, KM_CONV_NONE, h->p.empty};
   cudaEvent_t ev[6];
   for (auto& x : ev) KM_CUDA_TRY(cudaEventCreate(&x));
   double acc[5] = {0, 0, 0, 0, 0};

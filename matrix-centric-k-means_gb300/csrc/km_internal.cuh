@@ -67,6 +67,7 @@ struct LoopConsts {
   uint64_t maxiter;
   float tol;
   int32_t conv;       // km_conv
+  int32_t empty;      // km_empty
 };
 
 // ---------------------------------------------------------------------------

@@ -584,6 +584,9 @@ km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32
   return KM_OK;
 }
 
+// V.K, 4 sort kernels, c~, distances/argmin, control, label copy
+constexpr uint64_t KKM_KERNELS_PER_ITER = 9;
+
 km_status kkm_enqueue_iteration(km_kkm* h, const LoopConsts& lc) {
   LloydEngine& e = h->eng;
   const uint64_t n = h->p.n;
@@ -675,6 +678,14 @@ km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device) {
   return KM_OK;
 }
 
+km_status km_kkm_configure(km_kkm* h, uint64_t maxiter, float tol, int32_t check_converged) {
+  if (!h || maxiter == 0 || !(tol >= 0.0f)) return KM_ERR_ARG;
+  h->p.maxiter = maxiter;
+  h->p.tol = tol;
+  h->p.check_converged = check_converged != 0;
+  return KM_OK;
+}
+
 km_status km_kkm_fit(km_kkm* h, const uint32_t* init_labels, uint32_t* labels_out, km_result* res) {
   if (!h) return KM_ERR_ARG;
   if (!h->ready) return KM_ERR_STATE;
@@ -690,7 +701,7 @@ km_status km_kkm_fit(km_kkm* h, const uint32_t* init_labels, uint32_t* labels_ou
     round_robin_labels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, e.stream>>>(h->lab, n, h->p.k);
     KM_CUDA_TRY(cudaGetLastError());
   }
-  LoopConsts lc{h->p.maxiter, h->p.tol, h->p.check_converged ? KM_CONV_SCORE : KM_CONV_NONE};
+  LoopConsts lc{h->p.maxiter, h->p.tol, h->p.check_converged ? KM_CONV_SCORE : KM_CONV_NONE, 0};
   KM_CUDA_TRY(cudaEventRecord(h->ev0, e.stream));
   uint64_t launched = 0, batch = h->p.check_converged ? 4 : h->p.maxiter;
   while (launched < h->p.maxiter) {
@@ -718,6 +729,7 @@ km_status km_kkm_fit(km_kkm* h, const uint32_t* init_labels, uint32_t* labels_ou
     res->objective = s.objective;
     res->score = s.score;
     res->fit_ms = ms;
+    res->kernel_launches = launched * KKM_KERNELS_PER_ITER;
   }
   return KM_OK;
 }

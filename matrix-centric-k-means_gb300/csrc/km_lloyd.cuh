@@ -33,6 +33,7 @@ __global__ void seg_scatter_kernel(const uint32_t* labels, uint64_t n, uint32_t 
                                    uint32_t nseg, const uint32_t* seghist, const uint32_t* cstart,
                                    uint32_t* perm, DevState* st);
 __global__ void finalize_kernel(const float* Cn, float* C, const float* dsq, const double* objpart,
+                                const uint32_t* counts, int32_t empty_excl,
                                 uint32_t d, uint32_t dp, uint32_t k, float tol, float* cn2,
                                 __nv_bfloat16* Cb, __nv_bfloat16* Clo, float* Ct,
                                 double* shift_c, double* obj_c, DevState* st);

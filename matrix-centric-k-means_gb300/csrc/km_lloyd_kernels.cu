@@ -883,6 +883,7 @@ km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_
 // cluster, new ||c||^2 and BF16 copies; then C <- Cn.
 __global__ void finalize_kernel(const float* __restrict__ Cn, float* __restrict__ C,
                                 const float* __restrict__ dsq, const double* __restrict__ objpart,
+                                const uint32_t* __restrict__ counts, int32_t empty_excl,
                                 uint32_t d, uint32_t dp, uint32_t k, float tol,
                                 float* __restrict__ cn2, __nv_bfloat16* __restrict__ Cb,
                                 __nv_bfloat16* __restrict__ Clo, float* __restrict__ Ct,
@@ -893,6 +894,10 @@ __global__ void finalize_kernel(const float* __restrict__ Cn, float* __restrict_
   const int lane = threadIdx.x & 31;
   if (c >= k) return;
   const uint64_t base = (uint64_t)c * d;
+  // Reference GPU rule (src/kernels/distances.cu:588-599): an empty cluster's
+  // distance is +inf from then on, so it is never chosen again.  Its norm and
+  // its column of Ct become +inf; its (zero) centroid row stays finite.
+  const bool excl = empty_excl && counts[c] == 0u;
   double nrm = 0.0, mv = 0.0, ob = 0.0;
   for (uint32_t j = lane; j < dp; j += 32) {
     const float v = (j < d) ? Cn[base + j] : 0.0f;
@@ -901,7 +906,7 @@ __global__ void finalize_kernel(const float* __restrict__ Cn, float* __restrict_
       const double t = (double)v - (double)C[base + j];
       mv += t * t;
       ob += objpart[base + j];
-      Ct[(uint64_t)j * k + c] = v;
+      Ct[(uint64_t)j * k + c] = excl ? f_inf() : v;
     }
     if (Cb) {
       const __nv_bfloat16 hi = __float2bfloat16_rn(v);
@@ -918,7 +923,7 @@ __global__ void finalize_kernel(const float* __restrict__ Cn, float* __restrict_
     float s = 0.0f;
     for (uint32_t j = 0; j < d; ++j) s = __fadd_rn(s, dsq[base + j]);
     if (sqrtf(s) > tol) st->moved = 1u;
-    cn2[c] = (float)nrm;
+    cn2[c] = excl ? f_inf() : (float)nrm;
     shift_c[c] = sqrt(mv);
     obj_c[c] = ob;
   }
@@ -942,7 +947,8 @@ __global__ void control_kernel(const float* __restrict__ cn2, const double* __re
   for (uint32_t c = b; c < e; ++c) {
     ob += obj_c[c];
     sh = fmax(sh, shift_c[c]);
-    cm = fmaxf(cm, sqrtf(cn2[c]));
+    const float v = cn2[c];
+    if (v < f_inf()) cm = fmaxf(cm, sqrtf(v));   // excluded (empty) clusters hold +inf
   }
   s_obj[threadIdx.x] = ob; s_sh[threadIdx.x] = sh; s_cm[threadIdx.x] = cm;
   __syncthreads();

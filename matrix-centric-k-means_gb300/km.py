@@ -31,14 +31,15 @@ class LloydParams(C.Structure):
     _fields_ = [("n", C.c_uint64), ("d", C.c_uint32), ("k", C.c_uint32), ("tol", C.c_float),
                 ("seed", C.c_int32), ("maxiter", C.c_uint64), ("init", C.c_int32),
                 ("precision", C.c_int32), ("conv", C.c_int32), ("device", C.c_int32),
-                ("stream", C.c_void_p)]
+                ("stream", C.c_void_p), ("empty", C.c_int32)]
 
 
 class Result(C.Structure):
     _fields_ = [("converged_iter", C.c_uint64), ("iterations", C.c_uint64), ("converged", C.c_int32),
                 ("reserved0", C.c_int32), ("objective", C.c_double), ("score", C.c_double),
                 ("max_shift", C.c_double), ("refined_rows", C.c_uint64),
-                ("full_rescore_rows", C.c_uint64), ("fit_ms", C.c_double)]
+                ("full_rescore_rows", C.c_uint64), ("fit_ms", C.c_double),
+                ("kernel_launches", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved0"}
@@ -59,6 +60,9 @@ SIGNATURES = {
     "km_status_str": (C.c_char_p, [C.c_int]),
     "km_version": (C.c_char_p, []),
     "km_device_count": (C.c_int, []),
+    "km_mem_info": (C.c_int, [C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "km_lloyd_configure": (C.c_int, [C.c_void_p, C.c_uint64, C.c_float, C.c_int32]),
+    "km_kkm_configure": (C.c_int, [C.c_void_p, C.c_uint64, C.c_float, C.c_int32]),
     "km_lloyd_create": (C.c_int, [C.POINTER(LloydParams), C.POINTER(C.c_void_p)]),
     "km_lloyd_set_data": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "km_lloyd_fit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Result)]),
@@ -132,10 +136,11 @@ class Lloyd:
     """Handle over km_lloyd_*: the Kmeans(...) / run() / get_score() surface."""
 
     def __init__(self, n, d, k, tol=1e-4, seed=0, maxiter=300, init="sample", precision="fp32",
-                 conv="shift", device=0, stream=0):
+                 conv="shift", device=0, stream=0, empty="zero"):
         self.p = LloydParams(n, d, k, tol, seed, maxiter,
                              {"sample": INIT_SAMPLE, "round_robin": INIT_ROUND_ROBIN, "given": INIT_GIVEN}[init],
-                             PREC[precision], CONV[conv], device, stream or None)
+                             PREC[precision], CONV[conv], device, stream or None,
+                             {"zero": 0, "exclude": 1}[empty])
         h = C.c_void_p()
         check(_lib().km_lloyd_create(C.byref(self.p), C.byref(h)), "km_lloyd_create")
         self.h = h
