@@ -1,4 +1,5 @@
-"""Builds libkm_sm103.so (CUDA kernels + C ABI, sm_103a) and the gpukmeans CLI.
+"""Builds libkm_sm103.so (CUDA kernels + C ABI, sm_103a), libkmeans_host.so
+(the Kmeans class) and the gpukmeans CLI.
 
 Every translation unit is compiled in parallel: .cu files by nvcc for
 sm_103a only, .cpp files by g++.  Objects go to _build/, the library to lib/
@@ -82,13 +83,18 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     if _stale(lib, objs):
         logs.append(_run([nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a",
                           *map(str, objs), "-o", str(lib), "-lpthread"]))
-    # gpukmeans CLI (host C++ over the C ABI)
-    cli_src = sorted(HOST.glob("*.cpp"))
+    # host C++ over the C ABI: the Kmeans class library and the gpukmeans CLI
+    host_hdrs = sorted(inc.glob("*.hpp")) + sorted(inc.glob("*.h"))
+    host_srcs = [s for s in sorted(HOST.glob("*.cpp")) if s.name != "gpukmeans.cpp"]
+    hostlib = LIB / "libkmeans_host.so"
+    if host_srcs and _stale(hostlib, host_srcs + [lib] + host_hdrs):
+        logs.append(_run(["g++", *CXX_FLAGS, "-shared", "-I", str(inc), *map(str, host_srcs),
+                          "-o", str(hostlib), "-L", str(LIB), "-lkm_sm103", "-Wl,-rpath,$ORIGIN"]))
     cli = LIB / "gpukmeans"
-    if cli_src and _stale(cli, cli_src + sorted(HOST.glob("*.hpp")) + [lib]):
-        logs.append(_run(["g++", *CXX_FLAGS, "-I", str(inc), "-I", str(HOST), *map(str, cli_src),
-                          "-o", str(cli), "-L", str(LIB), "-lkm_sm103",
-                          f"-Wl,-rpath,$ORIGIN"]))
+    if (HOST / "gpukmeans.cpp").exists() and _stale(cli, [HOST / "gpukmeans.cpp", hostlib] + host_hdrs):
+        logs.append(_run(["g++", *CXX_FLAGS, "-I", str(inc), str(HOST / "gpukmeans.cpp"),
+                          "-o", str(cli), "-L", str(LIB), "-lkmeans_host", "-lkm_sm103",
+                          "-Wl,-rpath,$ORIGIN"]))
     if verbose:
         for l in logs:
             if l.strip():

@@ -6,7 +6,9 @@
 #   oracle/build_ref.sh [REFERENCE_ROOT]      (default: /root/reference)
 #
 # Only the reference's kmeans.cpp and its headers are compiled, together with
-# oracle/ref_shim.cpp (a C entry point).  The reference's main.cpp is not used:
+# oracle/ref_shim.cpp (a C entry point); the reference's header-only dataset
+# reader/writer (src/include/input_parser.hpp) is compiled with
+# oracle/ref_io_shim.cpp.  The reference's main.cpp is not used:
 # it calls a stale 11-argument parse_input_args (main.cpp:22) that no longer
 # matches utils.hpp:92-99.  -ffp-contract=off keeps every float operation
 # separately rounded, which is what the reference's makefile build does on
@@ -24,3 +26,7 @@ g++ -O2 -std=c++17 -ffp-contract=off -fPIC -shared -w \
     -I"$REF/src/include" -I"$REF/comparisons/CPU_Kmeans/include" \
     "$HERE/ref_shim.cpp" "$SRC" -o "$HERE/_ref/libref_kmeans.so"
 echo "built $HERE/_ref/libref_kmeans.so"
+# the reference's dataset reader/writer (header-only), behind C entry points
+g++ -O2 -std=c++17 -fPIC -shared -w -I"$REF/src/include" \
+    "$HERE/ref_io_shim.cpp" -o "$HERE/_ref/libref_io.so"
+echo "built $HERE/_ref/libref_io.so"

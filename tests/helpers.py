@@ -161,6 +161,61 @@ def ref_lloyd(X, k, tol, seed, maxiter):
     return int(it), lab
 
 
+_ref_io = None
+
+
+def reference_io_lib():
+    """oracle/_ref/libref_io.so: the reference's own dataset reader/writer
+    (src/include/input_parser.hpp) behind C entry points; None where the
+    reference tree is absent."""
+    global _ref_io
+    if _ref_io is None:
+        so = ORACLE / "_ref" / "libref_io.so"
+        if not so.exists() and REFERENCE.exists():
+            subprocess.run([str(ORACLE / "build_ref.sh"), str(REFERENCE)], check=True,
+                           capture_output=True)
+        if not so.exists():
+            return None
+        lib = C.CDLL(str(so))
+        vp, u64 = C.c_void_p, C.c_uint64
+        lib.ref_io_read.restype = None
+        lib.ref_io_read.argtypes = [C.c_char_p, u64, C.c_int, C.c_int, u64, vp]
+        lib.ref_io_random.restype = None
+        lib.ref_io_random.argtypes = [C.c_int, C.c_int, u64, vp]
+        lib.ref_io_to_csv.restype = u64
+        lib.ref_io_to_csv.argtypes = [vp, vp, C.c_int, u64, vp, u64]
+        _ref_io = lib
+    return _ref_io
+
+
+_host = None
+
+
+def host_lib():
+    """The product's host library (lib/libkmeans_host.so, km_host.h)."""
+    global _host
+    if _host is None:
+        so = PKG / "lib" / "libkmeans_host.so"
+        if not so.exists():
+            km().lib()   # raises with the build hint when nothing is built
+        lib = C.CDLL(str(so))
+        vp, u64, u32, i32 = C.c_void_p, C.c_uint64, C.c_uint32, C.c_int32
+        lib.kmh_read_points.restype = C.c_int
+        lib.kmh_read_points.argtypes = [C.c_char_p, u32, u64, i32, vp, C.POINTER(u64)]
+        lib.kmh_parse_points.restype = C.c_int
+        lib.kmh_parse_points.argtypes = [C.c_char_p, u64, i32, u32, u64, i32, vp, C.POINTER(u64)]
+        lib.kmh_random_points.restype = C.c_int
+        lib.kmh_random_points.argtypes = [i32, u32, u64, vp]
+        lib.kmh_write_csv.restype = C.c_int
+        lib.kmh_write_csv.argtypes = [C.c_char_p, vp, vp, u32, u64]
+        _host = lib
+    return _host
+
+
+def gpukmeans_bin():
+    return PKG / "lib" / "gpukmeans"
+
+
 def read_reference_csv(path, d):
     """The reference's CSV reader semantics (src/include/input_parser.hpp:103-131):
     header skipped, column 0 dropped, the next d columns read, missing -> 0."""
