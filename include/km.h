@@ -45,11 +45,15 @@ typedef enum km_status {
  * reference CPU k-means draws them (mt19937(seed_seq{seed}) +
  * uniform_int_distribution<int>(0,n-1), comparisons/CPU_Kmeans/src/kmeans.cpp:22-29,49-84).
  * KM_INIT_ROUND_ROBIN: labels i % k, as the reference GPU path
- * (src/kmeans.cu:365-374).  KM_INIT_GIVEN: caller-supplied centroids. */
+ * (src/kmeans.cu:365-374).  KM_INIT_GIVEN: caller-supplied centroids.
+ * KM_INIT_PLUSPLUS: greedy k-means++ on the device with s = 2 + ceil(ln k)
+ * D^2-sampled candidates per round (src/kmeans.cu:447-769), drawn from `seed`
+ * (the reference draws from std::random_device); k <= e^14. */
 typedef enum km_init {
   KM_INIT_SAMPLE = 0,
   KM_INIT_ROUND_ROBIN = 1,
-  KM_INIT_GIVEN = 2
+  KM_INIT_GIVEN = 2,
+  KM_INIT_PLUSPLUS = 3
 } km_init;
 
 /* Arithmetic of the distance stage.  FP32: SIMT FP32 GEMM.  BF16: tcgen05
@@ -151,6 +155,10 @@ km_status km_lloyd_set_data(km_lloyd* h, const float* X, int on_device);
  * (may be NULL); res may be NULL. */
 km_status km_lloyd_fit(km_lloyd* h, const float* C0, uint32_t* labels_out,
                        float* centroids_out, km_result* res);
+
+/* Runs only the configured initialisation and returns the k*d initial
+ * centroids (host array); C0 as in km_lloyd_fit. */
+km_status km_lloyd_init(km_lloyd* h, const float* C0, float* centroids_out);
 
 /* Changes the iteration budget and stop rule of a handle before its next fit
  * (Kmeans::run(maxiter, check_converged) sets both at run time,

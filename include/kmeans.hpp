@@ -7,7 +7,9 @@
 //     copies the points to the GPU (and, for a non-linear kernel, builds the
 //     n x n kernel matrix K = f(X X^T), src/kmeans.cu:143-211);
 //   run(maxiter, check_converged) starts from labels i % k
-//     (init_centroids_rand, src/kmeans.cu:365-374), iterates assignment and
+//     (init_centroids_rand, src/kmeans.cu:365-374) or, with plus_plus and the
+//     linear kernel, from greedy k-means++ centroids drawn from *seed
+//     (src/kmeans.cu:447-769), iterates assignment and
 //     update, stops on |score - last_score| < tol from the second iteration
 //     when check_converged (src/kmeans.cu:1063-1073) or after maxiter
 //     iterations, writes each point's label back with Point::setCluster
@@ -25,7 +27,8 @@
 // `level` (0..4, src/include/common.h:36-40) chose between the reference's
 // implementations of the same arithmetic; every level runs the same code here
 // and values outside 0..4 are rejected.  deviceProps is accepted and unused
-// (device 0, as the reference's main uses).
+// (device 0, as the reference's main uses).  plus_plus with a non-linear
+// kernel is rejected (KM_ERR_UNSUPPORTED).
 //
 // Errors: the reference exits the process (src/cuda_utils.cu:10-41); this
 // class throws KmeansError carrying the km_status instead, and the gpukmeans
@@ -98,7 +101,7 @@ class Kmeans {
   std::vector<double> profile_stages(uint64_t iters);
 
  private:
-  void setup(const float* X, InitMethod initMethod, Kernel kernel, int level,
+  void setup(const float* X, const int* seed, InitMethod initMethod, Kernel kernel, int level,
              Precision precision, const KernelParams& kp);
 
   size_t n;

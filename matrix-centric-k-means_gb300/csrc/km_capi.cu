@@ -134,6 +134,9 @@ km_status round_robin_init(LloydEngine& e) {
 }  // namespace
 }  // namespace km
 
+struct km_lloyd;
+static km_status run_init(km_lloyd* h, const float* C0);
+
 struct km_lloyd {
   km_lloyd_params p;
   LloydEngine eng;
@@ -144,6 +147,23 @@ struct km_lloyd {
   int32_t* h_done = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
+
+// Resets the loop state and places the initial centroids in e.C.
+static km_status run_init(km_lloyd* h, const float* C0) {
+  LloydEngine& e = h->eng;
+  KM_TRY(e.reset_state());
+  switch (h->p.init) {
+    case KM_INIT_SAMPLE: KM_TRY(sample_init(e, h->p.seed)); break;
+    case KM_INIT_ROUND_ROBIN: KM_TRY(round_robin_init(e)); break;
+    case KM_INIT_PLUSPLUS: KM_TRY(plusplus_init(e, h->p.seed)); break;
+    case KM_INIT_GIVEN:
+      if (!C0) return KM_ERR_ARG;
+      KM_CUDA_TRY(cudaMemcpyAsync(e.C, C0, sizeof(float) * e.k * e.d, cudaMemcpyHostToDevice, e.stream));
+      break;
+    default: return KM_ERR_ARG;
+  }
+  return e.set_centroids_dev(e.C);
+}
 
 extern "C" {
 
@@ -177,7 +197,7 @@ int km_device_count(void) {
 km_status km_lloyd_create(const km_lloyd_params* p, km_lloyd** out) {
   if (!p || !out) return KM_ERR_ARG;
   *out = nullptr;
-  if (p->init < KM_INIT_SAMPLE || p->init > KM_INIT_GIVEN) return KM_ERR_ARG;
+  if (p->init < KM_INIT_SAMPLE || p->init > KM_INIT_PLUSPLUS) return KM_ERR_ARG;
   if (p->conv < KM_CONV_SHIFT || p->conv > KM_CONV_NONE) return KM_ERR_ARG;
   if (p->empty != KM_EMPTY_ZERO && p->empty != KM_EMPTY_EXCLUDE) return KM_ERR_ARG;
   if (!(p->tol >= 0.0f) || p->maxiter == 0) return KM_ERR_ARG;
@@ -203,6 +223,17 @@ km_status km_mem_info(int32_t device, uint64_t* free_bytes, uint64_t* total_byte
   return KM_OK;
 }
 
+km_status km_lloyd_init(km_lloyd* h, const float* C0, float* centroids_out) {
+  if (!h || !centroids_out) return KM_ERR_ARG;
+  LloydEngine& e = h->eng;
+  if (!e.data_ready) return KM_ERR_STATE;
+  KM_CUDA_TRY(cudaSetDevice(e.device));
+  KM_TRY(run_init(h, C0));
+  KM_CUDA_TRY(cudaMemcpyAsync(centroids_out, e.C, sizeof(float) * e.k * e.d, cudaMemcpyDeviceToHost, e.stream));
+  KM_CUDA_TRY(cudaStreamSynchronize(e.stream));
+  return e.check_device_error();
+}
+
 km_status km_lloyd_configure(km_lloyd* h, uint64_t maxiter, float tol, int32_t conv) {
   if (!h || maxiter == 0 || !(tol >= 0.0f) || conv < KM_CONV_SHIFT || conv > KM_CONV_NONE) return KM_ERR_ARG;
   h->p.maxiter = maxiter;
@@ -222,17 +253,7 @@ km_status km_lloyd_fit(km_lloyd* h, const float* C0, uint32_t* labels_out, float
   LloydEngine& e = h->eng;
   if (!e.data_ready) return KM_ERR_STATE;
   KM_CUDA_TRY(cudaSetDevice(e.device));
-  KM_TRY(e.reset_state());
-  switch (h->p.init) {
-    case KM_INIT_SAMPLE: KM_TRY(sample_init(e, h->p.seed)); break;
-    case KM_INIT_ROUND_ROBIN: KM_TRY(round_robin_init(e)); break;
-    case KM_INIT_GIVEN:
-      if (!C0) return KM_ERR_ARG;
-      KM_CUDA_TRY(cudaMemcpyAsync(e.C, C0, sizeof(float) * e.k * e.d, cudaMemcpyHostToDevice, e.stream));
-      break;
-    default: return KM_ERR_ARG;
-  }
-  KM_TRY(e.set_centroids_dev(e.C));
+  KM_TRY(run_init(h, C0));
 
   LoopConsts lc{h->p.maxiter, h->p.tol, h->p.conv, h->p.empty};
   // One captured graph = G iterations; relaunched until the device says done.

@@ -131,4 +131,7 @@ struct LloydEngine {
   km_status check_device_error();
 };
 
+// Greedy k-means++ centroids into e.C (km_init.cu).
+km_status plusplus_init(LloydEngine& e, int seed);
+
 }  // namespace km

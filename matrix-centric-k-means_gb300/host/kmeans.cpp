@@ -19,7 +19,7 @@ km_precision to_prec(Kmeans::Precision p) {
 
 }  // namespace
 
-Kmeans::Kmeans(size_t n_, uint32_t d_, uint32_t k_, float tol_, const int* /*seed*/,
+Kmeans::Kmeans(size_t n_, uint32_t d_, uint32_t k_, float tol_, const int* seed,
                Point<float>** points, cudaDeviceProp* /*deviceProps*/, InitMethod initMethod,
                Kernel kernel, int level, Precision precision, KernelParams kparams)
     : n(n_), d(d_), k(k_), tol(tol_), points_(points) {
@@ -29,31 +29,31 @@ Kmeans::Kmeans(size_t n_, uint32_t d_, uint32_t k_, float tol_, const int* /*see
   std::vector<float> X(n * d);
   for (size_t i = 0; i < n; ++i)
     for (uint32_t j = 0; j < d; ++j) X[i * d + j] = points[i]->get(j);
-  setup(X.data(), initMethod, kernel, level, precision, kparams);
+  setup(X.data(), seed, initMethod, kernel, level, precision, kparams);
 }
 
-Kmeans::Kmeans(size_t n_, uint32_t d_, uint32_t k_, float tol_, const int* /*seed*/,
+Kmeans::Kmeans(size_t n_, uint32_t d_, uint32_t k_, float tol_, const int* seed,
                const float* X, uint32_t* labels_out, InitMethod initMethod, Kernel kernel,
                int level, Precision precision, KernelParams kparams)
     : n(n_), d(d_), k(k_), tol(tol_), labels_out_(labels_out) {
   if (!X) throw KmeansError(KM_ERR_ARG, "Kmeans: points");
-  setup(X, initMethod, kernel, level, precision, kparams);
+  setup(X, seed, initMethod, kernel, level, precision, kparams);
 }
 
-void Kmeans::setup(const float* X, InitMethod initMethod, Kernel kernel, int level,
+void Kmeans::setup(const float* X, const int* seed, InitMethod initMethod, Kernel kernel, int level,
                    Precision precision, const KernelParams& kp) {
   if (level < 0 || level > 4) throw KmeansError(KM_ERR_ARG, "Kmeans: level must be 0..4");
-  if (initMethod == InitMethod::plus_plus)
-    throw KmeansError(KM_ERR_UNSUPPORTED, "Kmeans: plus_plus initialisation");
+  if (initMethod == InitMethod::plus_plus && kernel != Kernel::linear)
+    throw KmeansError(KM_ERR_UNSUPPORTED, "Kmeans: plus_plus initialisation with a non-linear kernel");
   if (kernel == Kernel::linear) {
     km_lloyd_params p{};
     p.n = n;
     p.d = d;
     p.k = k;
     p.tol = tol;
-    p.seed = 0;
+    p.seed = seed ? *seed : 0;
     p.maxiter = 1;                       // set by run()
-    p.init = KM_INIT_ROUND_ROBIN;
+    p.init = initMethod == InitMethod::plus_plus ? KM_INIT_PLUSPLUS : KM_INIT_ROUND_ROBIN;
     p.precision = to_prec(precision);
     p.conv = KM_CONV_NONE;
     p.device = 0;

@@ -62,6 +62,7 @@ SIGNATURES = {
     "km_device_count": (C.c_int, []),
     "km_mem_info": (C.c_int, [C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "km_lloyd_configure": (C.c_int, [C.c_void_p, C.c_uint64, C.c_float, C.c_int32]),
+    "km_lloyd_init": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "km_kkm_configure": (C.c_int, [C.c_void_p, C.c_uint64, C.c_float, C.c_int32]),
     "km_lloyd_create": (C.c_int, [C.POINTER(LloydParams), C.POINTER(C.c_void_p)]),
     "km_lloyd_set_data": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
@@ -138,7 +139,8 @@ class Lloyd:
     def __init__(self, n, d, k, tol=1e-4, seed=0, maxiter=300, init="sample", precision="fp32",
                  conv="shift", device=0, stream=0, empty="zero"):
         self.p = LloydParams(n, d, k, tol, seed, maxiter,
-                             {"sample": INIT_SAMPLE, "round_robin": INIT_ROUND_ROBIN, "given": INIT_GIVEN}[init],
+                             {"sample": INIT_SAMPLE, "round_robin": INIT_ROUND_ROBIN, "given": INIT_GIVEN,
+                              "plusplus": 3}[init],
                              PREC[precision], CONV[conv], device, stream or None,
                              {"zero": 0, "exclude": 1}[empty])
         h = C.c_void_p()
@@ -165,6 +167,14 @@ class Lloyd:
                                   cents.ctypes.data if cents is not None else None, C.byref(r)),
               "km_lloyd_fit")
         return labels, cents, r
+
+    def init_centroids(self, C0=None):
+        """The configured initialisation alone (km_lloyd_init)."""
+        out = np.empty((self.p.k, self.p.d), np.float32)
+        c0 = None if C0 is None else np.ascontiguousarray(C0, dtype=np.float32)
+        check(_lib().km_lloyd_init(self.h, None if c0 is None else c0.ctypes.data, out.ctypes.data),
+              "km_lloyd_init")
+        return out
 
     def profile(self, iters):
         """Mean ms per iteration of the five stages (see km_lloyd_profile)."""

@@ -141,7 +141,11 @@ def test_cli_random_data_and_plusplus(gpu):
     out = run_cli("-n", 5000, "-d", 16, "-k", 8, "-m", 5, "-b", "random", "-f", "linear", "-l", 3, "-s", 3,
                   "-r", 2)
     parse_stdout(out, 2)
+    out = run_cli("-n", 5000, "-d", 16, "-k", 8, "-m", 50, "-t", 1e-3, "-c", 1, "-b", "plusplus", "-f", "linear",
+                  "-l", 3, "-s", 3, "-r", 2)
+    conv, _ = parse_stdout(out, 2)
+    assert conv[0] == conv[1]          # seeded: both runs identical
     exe = helpers.gpukmeans_bin()
-    r = subprocess.run([str(exe), "-n", "100", "-d", "2", "-k", "3", "-m", "5", "-b", "plusplus", "-f", "linear",
-                        "-l", "3"], capture_output=True, text=True, timeout=120)
-    assert r.returncode in (0, 1)
+    r = subprocess.run([str(exe), "-n", "100", "-d", "2", "-k", "3", "-m", "5", "-b", "plusplus", "-f",
+                        "polynomial", "-l", "3"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1 and "plus_plus" in r.stderr
