@@ -150,6 +150,12 @@ km_status km_lloyd_create(const km_lloyd_params* p, km_lloyd** out);
  * prepares the per-point data (norms, BF16 copies) once. */
 km_status km_lloyd_set_data(km_lloyd* h, const float* X, int on_device);
 
+/* Points stored as BF16 (n*d raw bit patterns, row-major; host pointer if
+ * on_device == 0).  The points ARE these BF16 values: they are widened once
+ * to FP32 (exact) for the re-score and the centroid update, and used as they
+ * are as the tensor-core operand. */
+km_status km_lloyd_set_data_bf16(km_lloyd* h, const uint16_t* X, int on_device);
+
 /* Runs the iteration.  C0: k*d host centroids for KM_INIT_GIVEN, else NULL.
  * labels_out: n host uint32 (may be NULL); centroids_out: k*d host floats
  * (may be NULL); res may be NULL. */

@@ -242,6 +242,11 @@ km_status km_lloyd_configure(km_lloyd* h, uint64_t maxiter, float tol, int32_t c
   return KM_OK;
 }
 
+km_status km_lloyd_set_data_bf16(km_lloyd* h, const uint16_t* X, int on_device) {
+  if (!h || !X) return KM_ERR_ARG;
+  return h->eng.set_points_bf16(X, on_device != 0);
+}
+
 km_status km_lloyd_set_data(km_lloyd* h, const float* X, int on_device) {
   if (!h || !X) return KM_ERR_ARG;
   return h->eng.set_points(X, on_device != 0, true);

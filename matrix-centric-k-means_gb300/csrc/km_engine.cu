@@ -100,7 +100,12 @@ km_status LloydEngine::init(uint64_t n_, uint32_t d_, uint32_t k_, int precision
   dp = round_up(d, 64);
   kp = round_up(std::max<uint32_t>(k, 16), 16);
   if (precision != KM_PREC_FP32) {
-    tc = plan_tc(dp, kp, precision == KM_PREC_BF16X3, n, num_sms);
+    if (kp <= 256) tc = plan_tc(dp, kp, precision == KM_PREC_BF16X3, n, num_sms);
+    if (!tc.ok) {
+      // k > 256, or the centroid operand does not fit shared memory whole
+      tc = plan_tc_chunked(dp, k, precision == KM_PREC_BF16X3, n, num_sms);
+      if (tc.ok) kp = tc.kp;            // centroid operand padded to whole chunks
+    }
     if (!tc.ok) return KM_ERR_UNSUPPORTED;
     KM_TRY(tc_set_attributes(tc, precision == KM_PREC_BF16X3));
   }
@@ -186,10 +191,11 @@ km_status LloydEngine::set_points(const float* Xsrc, bool on_device, bool copy) 
   KM_CUDA_TRY(cudaGetLastError());
   if (precision != KM_PREC_FP32) {
     KM_TRY(encode_tmap_bf16(&tmA, Xb, dp, n, 64, 128));
-    KM_TRY(encode_tmap_bf16(&tmB, Cb, dp, kp, 64, kp));
+    const uint32_t bbox = tc.chunked ? tc.NC : kp;    // rows of one B load
+    KM_TRY(encode_tmap_bf16(&tmB, Cb, dp, kp, 64, bbox));
     if (precision == KM_PREC_BF16X3) {
       KM_TRY(encode_tmap_bf16(&tmAlo, Xlo, dp, n, 64, 128));
-      KM_TRY(encode_tmap_bf16(&tmBlo, Clo, dp, kp, 64, kp));
+      KM_TRY(encode_tmap_bf16(&tmBlo, Clo, dp, kp, 64, bbox));
     } else {
       tmAlo = tmA;
       tmBlo = tmB;
@@ -199,6 +205,39 @@ km_status LloydEngine::set_points(const float* Xsrc, bool on_device, bool copy) 
   if (h_st->err & KM_DEVERR_NONFINITE) return KM_ERR_ARG;
   data_ready = true;
   return KM_OK;
+}
+
+namespace {
+__global__ void bf16_decode_kernel(const uint16_t* __restrict__ src, uint64_t count, float* __restrict__ dst) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = __uint_as_float((uint32_t)src[i] << 16);
+}
+}  // namespace
+
+km_status LloydEngine::set_points_bf16(const uint16_t* Xsrc, bool on_device) {
+  KM_CUDA_TRY(cudaSetDevice(device));
+  if (!X_owned) KM_TRY(dalloc(&X_owned, (size_t)n * d));
+  const uint64_t count = n * (uint64_t)d;
+  const uint16_t* src = Xsrc;
+  uint16_t* tmp = nullptr;
+  if (!on_device) {
+    // host BF16 bits go to a staging buffer (half the bytes of the FP32 copy)
+    KM_TRY(dalloc(&tmp, count));
+    KM_CUDA_TRY(cudaMemcpyAsync(tmp, Xsrc, sizeof(uint16_t) * count, cudaMemcpyHostToDevice, stream));
+    src = tmp;
+  }
+  const unsigned blocks = (unsigned)std::min<uint64_t>((count + 255) / 256, (uint64_t)num_sms * 32);
+  bf16_decode_kernel<<<blocks, 256, 0, stream>>>(src, count, X_owned);
+  cudaError_t le = cudaGetLastError();
+  if (tmp) {
+    cudaError_t se = cudaStreamSynchronize(stream);
+    cudaFree(tmp);
+    KM_CUDA_TRY(le);
+    KM_CUDA_TRY(se);
+  }
+  KM_CUDA_TRY(le);
+  return set_points(X_owned, true, false);
 }
 
 km_status LloydEngine::reset_state() {

@@ -43,13 +43,18 @@ __global__ void control_kernel(const float* cn2, const double* shift_c, const do
 // ---- tensor-core distance stage (km_tc.cu) ----
 struct TcPlan {
   bool ok = false;
+  bool chunked = false;  // k > 256: centroids walked in chunks of NC (assign_tc_chunked_kernel)
   uint32_t KB = 0;       // K blocks of 64 columns
   uint32_t stages = 0;   // A pipeline depth (K-block units)
   uint32_t nalloc = 0;   // TMEM columns per accumulator buffer
+  uint32_t NC = 0;       // chunked: centroids per chunk (128 or 256)
+  uint32_t T = 0;        // chunked: tiles per CTA per band (even)
+  uint32_t kp = 0;       // chunked: k padded to a multiple of NC
   size_t smem = 0;       // dynamic shared memory bytes
   int grid = 0;
 };
 TcPlan plan_tc(uint32_t dp, uint32_t kp, bool x3, uint64_t n, int num_sms);
+TcPlan plan_tc_chunked(uint32_t dp, uint32_t k, bool x3, uint64_t n, int num_sms);
 km_status encode_tmap_bf16(CUtensorMap* tm, const void* base, uint64_t inner, uint64_t outer,
                            uint32_t box_inner, uint32_t box_outer);
 km_status tc_set_attributes(const TcPlan& pl, bool x3);
@@ -118,6 +123,9 @@ struct LloydEngine {
   km_status init(uint64_t n, uint32_t d, uint32_t k, int precision, int device, void* stream,
                  bool need_update);
   km_status set_points(const float* Xsrc, bool on_device, bool copy);
+  // Points stored as BF16 (raw bit patterns, n*d): decoded once to the FP32
+  // copy, which is then exactly representable in BF16 (Xb = the input).
+  km_status set_points_bf16(const uint16_t* Xsrc, bool on_device);
   km_status set_centroids_dev(const float* Csrc_dev);   // C <- src, prep norms/bf16, cmax
   km_status reset_state();
   km_status enqueue_distance(float* Dout);   // distance + argmin kernel only

@@ -36,6 +36,8 @@
 
 #include <cudaTypedefs.h>
 
+#include <algorithm>
+
 namespace km {
 
 namespace {
@@ -282,6 +284,360 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   if (warp == 2) tmem_dealloc(tmem_base, 2u * nalloc);
 }
 
+
+// ---------------------------------------------------------------------------
+// k > 256: the centroid operand no longer fits one MMA (N <= 256) nor shared
+// memory, so it is walked in chunks of NC (256 or 128) centroids.
+//
+// Rows are processed in bands of gridDim.x * T tiles (T even, a band of X
+// stays in L2): for each band every CTA takes its T tiles and, for each
+// chunk j, loads chunk j of the centroids (one B slot per 64-column K block,
+// each slot reloaded as soon as the MMAs of the previous chunk have read it)
+// and runs its T tiles against it.  Each row keeps a running state across the
+// chunks in shared memory: the running minimum m and up to four candidates
+// (index, value) with value <= tau(m); when a chunk lowers m the list is
+// filtered with the new tau (tau grows with m, so what survives is exactly
+// {c : v(c) <= tau(m)} over the chunks seen), and more than four candidates
+// marks the row for the full re-score.  After the last chunk the row gets the
+// same treatment as in the single-chunk kernel: one candidate = proven label,
+// 2..4 = exact re-score of those, otherwise full re-score.
+//
+// Tile i of a band always goes to epilogue set i % 2 and TMEM buffer i % 2,
+// so a row's state is only touched by one thread.
+// ---------------------------------------------------------------------------
+constexpr uint32_t TCC_OVF = 0xffu;     // candidate list overflowed
+
+struct TcSmemC {
+  uint64_t full[16];
+  uint64_t empty[16];
+  uint64_t bfull[8];
+  uint64_t bempty[8];
+  uint64_t tfull[2];
+  uint64_t tempty[2];
+  uint64_t tdone;
+  uint32_t tmem_base;
+  int abort;
+};
+
+__host__ __device__ constexpr uint32_t tcc_state_bytes(uint32_t T) { return T * TC_M * 40u; }
+
+template <bool X3>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
+                         const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo,
+                         const float* __restrict__ cn2, const float* __restrict__ xn2, uint64_t n,
+                         uint32_t k, uint32_t kp, uint32_t NC, uint32_t KB, uint32_t S, uint32_t T,
+                         TieBound tb, DevState* st, uint32_t* __restrict__ labels,
+                         float* __restrict__ mindist, RefineQueues rq, float* __restrict__ Dout) {
+  if (st->done) return;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  const uint32_t slot_bytes = NC * 128u;                // one 64-column K block of NC centroids
+  const uint32_t b_bytes = KB * slot_bytes;             // one of hi / lo
+  uint8_t* sB = smem;
+  uint8_t* sA = smem + b_bytes * (X3 ? 2u : 1u);
+  const uint32_t unit_bytes = A_UNIT * (X3 ? 2u : 1u);
+  uint8_t* sState = sA + (size_t)S * unit_bytes;
+  const uint32_t rows_T = T * TC_M;
+  float* st_m = reinterpret_cast<float*>(sState);
+  uint32_t* st_cnt = reinterpret_cast<uint32_t*>(st_m + rows_T);
+  uint32_t* st_c = st_cnt + rows_T;                     // [4][rows_T]
+  float* st_v = reinterpret_cast<float*>(st_c + 4u * rows_T);
+  TcSmemC* ts = reinterpret_cast<TcSmemC*>(sState + tcc_state_bytes(T));
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint64_t ntiles = (n + TC_M - 1) / TC_M;
+  const uint32_t nchunks = kp / NC;
+  const uint64_t band_tiles = (uint64_t)gridDim.x * T;
+  const float cmax = st->cmax;
+  // valid tiles of this CTA in band b: i = 0..Tc-1 (tile = b*band_tiles + i*gridDim.x + blockIdx.x)
+  auto tiles_in_band = [&](uint64_t b) -> uint32_t {
+    const uint64_t first = b * band_tiles + blockIdx.x;
+    if (first >= ntiles) return 0u;
+    const uint64_t c = (ntiles - first + gridDim.x - 1) / gridDim.x;
+    return (uint32_t)(c < T ? c : T);
+  };
+  auto tile_of = [&](uint64_t b, uint32_t i) -> uint64_t {
+    return b * band_tiles + (uint64_t)i * gridDim.x + blockIdx.x;
+  };
+
+  if (threadIdx.x == 0) {
+    for (uint32_t s = 0; s < S; ++s) { mbar_init(&ts->full[s], 1); mbar_init(&ts->empty[s], 1); }
+    for (uint32_t kb = 0; kb < KB; ++kb) { mbar_init(&ts->bfull[kb], 1); mbar_init(&ts->bempty[kb], 1); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], 4); }
+    mbar_init(&ts->tdone, 1);
+    ts->abort = 0;
+    mbar_fence_init();
+  }
+  if (warp == 2) tmem_alloc(&ts->tmem_base, 2u * NC);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = ts->tmem_base;
+  volatile int* abort_flag = &ts->abort;
+
+  auto fail = [&](uint32_t where) {
+    ts->abort = 1;
+    if (atomicOr(&st->err, KM_DEVERR_TIMEOUT) == 0u) st->err_where = where;
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      if (X3) { tma_prefetch_desc(&tmAlo); tma_prefetch_desc(&tmBlo); }
+      uint64_t u = 0, p = 0;
+      bool ok = true;
+      for (uint64_t b = 0; ok; ++b) {
+        const uint32_t Tc = tiles_in_band(b);
+        if (Tc == 0u) break;
+        for (uint32_t j = 0; j < nchunks && ok; ++j, ++p) {
+          for (uint32_t kb = 0; kb < KB; ++kb) {
+            if (p > 0 && !mbar_wait_bounded(&ts->bempty[kb], (uint32_t)((p - 1) & 1u), abort_flag, WAIT_NS)) {
+              fail(11); ok = false; break;
+            }
+            mbar_arrive_expect_tx(&ts->bfull[kb], slot_bytes * (X3 ? 2u : 1u));
+            tma_load_2d(sB + (size_t)kb * slot_bytes, &tmB, (int)(kb * 64), (int)(j * NC), &ts->bfull[kb]);
+            if (X3) tma_load_2d(sB + b_bytes + (size_t)kb * slot_bytes, &tmBlo, (int)(kb * 64), (int)(j * NC),
+                                &ts->bfull[kb]);
+          }
+          for (uint32_t i = 0; i < Tc && ok; ++i) {
+            const uint64_t tile = tile_of(b, i);
+            for (uint32_t kb = 0; kb < KB; ++kb, ++u) {
+              const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
+              if (!mbar_wait_bounded(&ts->empty[s], ph ^ 1u, abort_flag, WAIT_NS)) { fail(12); ok = false; break; }
+              mbar_arrive_expect_tx(&ts->full[s], unit_bytes);
+              uint8_t* dst = sA + (size_t)s * unit_bytes;
+              tma_load_2d(dst, &tmA, (int)(kb * 64), (int)(tile * TC_M), &ts->full[s]);
+              if (X3) tma_load_2d(dst + A_UNIT, &tmAlo, (int)(kb * 64), (int)(tile * TC_M), &ts->full[s]);
+            }
+          }
+        }
+      }
+      // Drain every issued copy before the CTA exits (bounded, abort ignored).
+      volatile int no_abort = 0;
+      if (p > 0)
+        for (uint32_t kb = 0; kb < KB; ++kb) mbar_wait_bounded(&ts->bfull[kb], (uint32_t)((p - 1) & 1u), &no_abort, WAIT_NS);
+      const uint64_t first = u > S ? u - S : 0;
+      for (uint64_t v = first; v < u; ++v) {
+        const uint32_t s = (uint32_t)(v % S), ph = (uint32_t)((v / S) & 1u);
+        mbar_wait_bounded(&ts->full[s], ph, &no_abort, WAIT_NS);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(TC_M, NC);
+      const uint32_t sA0 = smem_u32(sA), sB0 = smem_u32(sB);
+      uint64_t u = 0, p = 0;
+      uint32_t use0 = 0u, use1 = 0u;                 // items issued on TMEM buffer 0 / 1
+      bool ok = true, issued = false;
+      for (uint64_t b = 0; ok; ++b) {
+        const uint32_t Tc = tiles_in_band(b);
+        if (Tc == 0u) break;
+        for (uint32_t j = 0; j < nchunks && ok; ++j, ++p) {
+          for (uint32_t i = 0; i < Tc && ok; ++i) {
+            const uint32_t buf = i & 1u;
+            const uint32_t ub = buf ? use1 : use0;
+            if (!mbar_wait_bounded(&ts->tempty[buf], (ub & 1u) ^ 1u, abort_flag, WAIT_NS)) {
+              fail(13); ok = false; break;
+            }
+            if (buf) ++use1; else ++use0;
+            tc_fence_after();
+            const uint32_t dt = tmem_base + buf * NC;
+            for (uint32_t kb = 0; kb < KB; ++kb, ++u) {
+              if (i == 0u) {
+                if (!mbar_wait_bounded(&ts->bfull[kb], (uint32_t)(p & 1u), abort_flag, WAIT_NS)) {
+                  fail(14); ok = false; break;
+                }
+              }
+              const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
+              if (!mbar_wait_bounded(&ts->full[s], ph, abort_flag, WAIT_NS)) { fail(15); ok = false; break; }
+              tc_fence_after();
+              const uint32_t a0 = sA0 + s * unit_bytes;
+              const uint32_t b0 = sB0 + kb * slot_bytes;
+#pragma unroll
+              for (uint32_t kk = 0; kk < 4; ++kk) {
+                const uint64_t ad = smem_desc_sw128(a0 + kk * 32u);
+                const uint64_t bd = smem_desc_sw128(b0 + kk * 32u);
+                tc_mma_bf16(dt, ad, bd, idesc, (kb | kk) != 0u ? 1u : 0u);
+                if (X3) {
+                  const uint64_t adl = smem_desc_sw128(a0 + A_UNIT + kk * 32u);
+                  const uint64_t bdl = smem_desc_sw128(b0 + b_bytes + kk * 32u);
+                  tc_mma_bf16(dt, ad, bdl, idesc, 1u);
+                  tc_mma_bf16(dt, adl, bd, idesc, 1u);
+                }
+              }
+              tc_commit(&ts->empty[s]);
+              if (i + 1u == Tc) tc_commit(&ts->bempty[kb]);   // B slot kb free once these complete
+              issued = true;
+            }
+            if (!ok) break;
+            tc_commit(&ts->tfull[buf]);
+          }
+        }
+      }
+      if (issued) {
+        tc_commit(&ts->tdone);
+        volatile int no_abort = 0;
+        mbar_wait_bounded(&ts->tdone, 0, &no_abort, WAIT_NS);
+      }
+    }
+  } else if (warp >= 4) {
+    const int q = warp & 3;
+    const uint32_t set = (uint32_t)(warp - 4) >> 2;
+    const uint32_t npair = NC / 64u;
+    const uint32_t r = (uint32_t)q * 32u + (uint32_t)lane;
+    const uint32_t tbase = tmem_base + (((uint32_t)q * 32u) << 16) + set * NC;
+    const float finf = __int_as_float(0x7f800000);
+    uint32_t use = 0;
+    bool ok = true;
+    for (uint64_t b = 0; ok; ++b) {
+      const uint32_t Tc = tiles_in_band(b);
+      if (Tc == 0u) break;
+      for (uint32_t j = 0; j < nchunks && ok; ++j) {
+        const bool last = (j + 1u == nchunks);
+        for (uint32_t i = set; i < Tc; i += 2u) {
+          const uint64_t row = tile_of(b, i) * TC_M + r;
+          const bool valid = row < n;
+          const float x2 = valid ? xn2[row] : 0.0f;
+          const uint32_t si = i * TC_M + r;
+          float m = finf;
+          uint32_t cnt = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+          float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
+          if (j > 0) {
+            m = st_m[si]; cnt = st_cnt[si];
+            c0 = st_c[si]; c1 = st_c[rows_T + si]; c2 = st_c[2 * rows_T + si]; c3 = st_c[3 * rows_T + si];
+            v0 = st_v[si]; v1 = st_v[rows_T + si]; v2 = st_v[2 * rows_T + si]; v3 = st_v[3 * rows_T + si];
+          }
+          const bool okw = mbar_wait_bounded(&ts->tfull[set], use & 1u, abort_flag, WAIT_NS);
+          ++use;
+          if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(16); ok = false; break; }
+          tc_fence_after();
+          const float* cnj = cn2 + (size_t)j * NC;
+          // ---- pass 1: chunk minimum ----
+          float m0 = finf, m1 = finf, m2 = finf, m3 = finf;
+          for (uint32_t pr = 0; pr < npair; ++pr) {
+            uint32_t acc[64];
+            tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
+            tmem_ld_wait();
+            const float4* cn4 = reinterpret_cast<const float4*>(cnj + pr * 64u);
+#pragma unroll
+            for (int j4 = 0; j4 < 16; ++j4) {
+              const float4 cc = __ldg(cn4 + j4);
+              m0 = fminf(m0, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 0]), cc.x));
+              m1 = fminf(m1, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 1]), cc.y));
+              m2 = fminf(m2, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 2]), cc.z));
+              m3 = fminf(m3, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 3]), cc.w));
+            }
+          }
+          const float mc = fminf(fminf(m0, m1), fminf(m2, m3));
+          const float mn = fminf(m, mc);
+          const float tau = tie_tau(x2, mn, cmax, tb);
+          // ---- filter the running list with the new tau (keeps ascending order) ----
+          if (cnt != TCC_OVF) {
+            uint32_t nk = 0, e0 = 0, e1 = 0, e2 = 0, e3 = 0;
+            float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;
+            const uint32_t ci[4] = {c0, c1, c2, c3};
+            const float cv[4] = {v0, v1, v2, v3};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              if ((uint32_t)e < cnt && cv[e] <= tau) {
+                e0 = (nk == 0) ? ci[e] : e0; w0 = (nk == 0) ? cv[e] : w0;
+                e1 = (nk == 1) ? ci[e] : e1; w1 = (nk == 1) ? cv[e] : w1;
+                e2 = (nk == 2) ? ci[e] : e2; w2 = (nk == 2) ? cv[e] : w2;
+                e3 = (nk == 3) ? ci[e] : e3; w3 = (nk == 3) ? cv[e] : w3;
+                ++nk;
+              }
+            }
+            cnt = nk; c0 = e0; c1 = e1; c2 = e2; c3 = e3; v0 = w0; v1 = w1; v2 = w2; v3 = w3;
+          }
+          // ---- pass 2: this chunk's candidates {c < k : v(c) <= tau} ----
+          const bool collect = tau < finf;                 // tau = +inf only while every value is +inf
+          for (uint32_t pr = 0; pr < npair; ++pr) {
+            uint32_t acc[64];
+            tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
+            tmem_ld_wait();
+            const float4* cn4 = reinterpret_cast<const float4*>(cnj + pr * 64u);
+            uint32_t mlo = 0, mhi = 0;
+#pragma unroll
+            for (int j4 = 0; j4 < 8; ++j4) {
+              const float4 cc = __ldg(cn4 + j4);
+              if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 0]), cc.x) <= tau) mlo |= 1u << (4 * j4 + 0);
+              if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 1]), cc.y) <= tau) mlo |= 1u << (4 * j4 + 1);
+              if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 2]), cc.z) <= tau) mlo |= 1u << (4 * j4 + 2);
+              if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 3]), cc.w) <= tau) mlo |= 1u << (4 * j4 + 3);
+            }
+#pragma unroll
+            for (int j4 = 0; j4 < 8; ++j4) {
+              const float4 cc = __ldg(cn4 + 8 + j4);
+              if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 0]), cc.x) <= tau) mhi |= 1u << (4 * j4 + 0);
+              if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 1]), cc.y) <= tau) mhi |= 1u << (4 * j4 + 1);
+              if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 2]), cc.z) <= tau) mhi |= 1u << (4 * j4 + 2);
+              if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 3]), cc.w) <= tau) mhi |= 1u << (4 * j4 + 3);
+            }
+            const uint32_t mm[2] = {mlo, mhi};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const uint32_t col0 = j * NC + pr * 64u + (uint32_t)h * 32u;     // global centroid index
+              uint32_t mk = collect ? mm[h] : 0u;
+              mk &= (col0 >= k) ? 0u : (k - col0 >= 32u ? 0xffffffffu : ((1u << (k - col0)) - 1u));
+              while (mk != 0u) {
+                const uint32_t bit = (uint32_t)(__ffs(mk) - 1);
+                mk &= mk - 1u;
+                if (cnt == TCC_OVF) break;
+                if (cnt == 4u) { cnt = TCC_OVF; break; }
+                const uint32_t col = col0 + bit;
+                // the candidate's accumulator by selection (static register indices)
+                uint32_t a = 0u;
+#pragma unroll
+                for (int jj = 0; jj < 32; ++jj) a = ((uint32_t)jj == bit) ? acc[h * 32 + jj] : a;
+                const float vv = fmaf(-2.0f, __uint_as_float(a), __ldg(cnj + pr * 64u + h * 32u + bit));
+                c0 = (cnt == 0) ? col : c0; v0 = (cnt == 0) ? vv : v0;
+                c1 = (cnt == 1) ? col : c1; v1 = (cnt == 1) ? vv : v1;
+                c2 = (cnt == 2) ? col : c2; v2 = (cnt == 2) ? vv : v2;
+                c3 = (cnt == 3) ? col : c3; v3 = (cnt == 3) ? vv : v3;
+                ++cnt;
+              }
+            }
+            if (Dout && valid) {
+#pragma unroll
+              for (int jj = 0; jj < 64; ++jj) {
+                const uint32_t col = j * NC + pr * 64u + (uint32_t)jj;
+                if (col < k) Dout[row * k + col] = fmaf(-2.0f, __uint_as_float(acc[jj]), cnj[pr * 64u + jj]) + x2;
+              }
+            }
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&ts->tempty[set]);     // accumulator buffer free
+          if (!last) {
+            st_m[si] = mn; st_cnt[si] = cnt;
+            st_c[si] = c0; st_c[rows_T + si] = c1; st_c[2 * rows_T + si] = c2; st_c[3 * rows_T + si] = c3;
+            st_v[si] = v0; st_v[rows_T + si] = v1; st_v[2 * rows_T + si] = v2; st_v[3 * rows_T + si] = v3;
+          } else {
+            // NaN anywhere leaves cnt == 0; overflow or no candidate: full re-score.
+            const uint32_t cf = (cnt == TCC_OVF) ? 0xffffffffu : cnt;
+            if (valid) {
+              labels[row] = c0;
+              if (mindist) mindist[row] = mn + x2;
+            }
+            RefineEntry e{(uint32_t)row, cf, {c0, c1, c2, c3}};
+            const uint64_t seg = row >> 5;
+            seg_push(rq.cand, rq.ccnt, seg, valid && cf >= 2u && cf <= 4u, e);
+            seg_push(rq.full, rq.fcnt, seg, valid && (cf == 0u || cf > 4u), (uint32_t)row);
+          }
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 2) tmem_dealloc(tmem_base, 2u * NC);
+}
+
 }  // namespace
 
 TcPlan plan_tc(uint32_t dp, uint32_t kp, bool x3, uint64_t n, int num_sms) {
@@ -329,8 +685,52 @@ km_status encode_tmap_bf16(CUtensorMap* tm, const void* base, uint64_t inner, ui
   return r == CUDA_SUCCESS ? KM_OK : KM_ERR_CUDA;
 }
 
+TcPlan plan_tc_chunked(uint32_t dp, uint32_t k, bool x3, uint64_t n, int num_sms) {
+  TcPlan p;
+  if (dp == 0 || dp % 64 != 0 || k == 0) return p;
+  const uint32_t KB = dp / 64;
+  if (KB > 8) return p;
+  const size_t mult = x3 ? 2 : 1;
+  const size_t unit = (size_t)A_UNIT * mult;
+  const size_t budget = 227 * 1024;
+  const size_t band_max = 48ull << 20;             // rows of one band stay in L2
+  for (uint32_t NC : {256u, 128u}) {
+    if (NC == 256u && k <= 128u) continue;         // one 128-wide chunk wastes less
+    const size_t b_bytes = (size_t)KB * NC * 128 * mult;
+    for (uint32_t T : {8u, 6u, 4u, 2u}) {
+      const size_t band = (size_t)num_sms * T * TC_M * dp * 2 * mult;
+      if (band > band_max && T > 2) continue;
+      const size_t fixed = 1024 + b_bytes + tcc_state_bytes(T) + sizeof(TcSmemC) + 64;
+      if (fixed + 2 * unit > budget) continue;
+      size_t s = (budget - fixed) / unit;
+      if (s > 8) s = 8;
+      p.chunked = true;
+      p.KB = KB;
+      p.NC = NC;
+      p.T = T;
+      p.kp = (k + NC - 1) / NC * NC;
+      p.stages = (uint32_t)s;
+      p.nalloc = NC;
+      p.smem = fixed + s * unit;
+      const uint64_t ntiles = (n + TC_M - 1) / TC_M;
+      p.grid = (int)std::min<uint64_t>(ntiles, (uint64_t)num_sms);
+      if (p.grid < 1) p.grid = 1;
+      p.ok = true;
+      return p;
+    }
+  }
+  return p;
+}
+
 km_status tc_set_attributes(const TcPlan& pl, bool x3) {
   if (!pl.ok) return KM_ERR_UNSUPPORTED;
+  if (pl.chunked) {
+    if (x3)
+      KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_chunked_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+    else
+      KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_chunked_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+    return KM_OK;
+  }
   if (x3)
     KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
   else
@@ -345,6 +745,18 @@ km_status launch_assign_tc(const TcPlan& pl, bool x3, const CUtensorMap& tmA,
                            uint32_t* labels, float* mindist, const RefineQueues& rq,
                            float* Dout, cudaStream_t s) {
   if (!pl.ok) return KM_ERR_UNSUPPORTED;
+  if (pl.chunked) {
+    if (x3)
+      assign_tc_chunked_kernel<true><<<pl.grid, TC_THREADS, pl.smem, s>>>(
+          tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.NC, pl.KB, pl.stages, pl.T, tb, st, labels,
+          mindist, rq, Dout);
+    else
+      assign_tc_chunked_kernel<false><<<pl.grid, TC_THREADS, pl.smem, s>>>(
+          tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.NC, pl.KB, pl.stages, pl.T, tb, st, labels,
+          mindist, rq, Dout);
+    KM_CUDA_TRY(cudaGetLastError());
+    return KM_OK;
+  }
   if (x3) {
     assign_tc_kernel<true><<<pl.grid, TC_THREADS, pl.smem, s>>>(
         tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.KB, pl.stages, pl.nalloc, tb, st, labels,

@@ -63,6 +63,7 @@ SIGNATURES = {
     "km_mem_info": (C.c_int, [C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "km_lloyd_configure": (C.c_int, [C.c_void_p, C.c_uint64, C.c_float, C.c_int32]),
     "km_lloyd_init": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "km_lloyd_set_data_bf16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "km_kkm_configure": (C.c_int, [C.c_void_p, C.c_uint64, C.c_float, C.c_int32]),
     "km_lloyd_create": (C.c_int, [C.POINTER(LloydParams), C.POINTER(C.c_void_p)]),
     "km_lloyd_set_data": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
@@ -153,6 +154,16 @@ class Lloyd:
             check(_lib().km_lloyd_set_data(self.h, X.ctypes.data, 0), "km_lloyd_set_data")
         else:
             check(_lib().km_lloyd_set_data(self.h, X.data_ptr(), 1), "km_lloyd_set_data")
+        return self
+
+    def set_data_bf16(self, Xbits):
+        """Points stored as BF16: a uint16 numpy array of the bit patterns, or a
+        torch.bfloat16 / int16 device tensor."""
+        if isinstance(Xbits, np.ndarray):
+            Xbits = np.ascontiguousarray(Xbits, dtype=np.uint16)
+            check(_lib().km_lloyd_set_data_bf16(self.h, Xbits.ctypes.data, 0), "km_lloyd_set_data_bf16")
+        else:
+            check(_lib().km_lloyd_set_data_bf16(self.h, Xbits.data_ptr(), 1), "km_lloyd_set_data_bf16")
         return self
 
     def fit(self, C0=None, want_centroids=True):

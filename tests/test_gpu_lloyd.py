@@ -33,12 +33,6 @@ def case_data(c):
 @pytest.mark.parametrize("c", CASES, ids=[c["name"] for c in CASES])
 def test_lloyd_matches_reference_golden(km, gpu, c, prec):
     X = case_data(c)
-    if prec == "bf16x3" and c["name"] == "d200_k256":
-        # hi+lo centroid operand (256 x 256 x 2 x 2 B) exceeds shared memory: reported, not faked
-        with pytest.raises(km.KmError) as e:
-            km.Lloyd(c["n"], c["d"], c["k"], precision=prec)
-        assert e.value.status == km.KM_ERR_UNSUPPORTED
-        return
     m = km.Lloyd(c["n"], c["d"], c["k"], tol=c["tol"], seed=c["seed"], maxiter=c["maxiter"],
                  precision=prec).set_data(X)
     lab, cen, r = m.fit()
@@ -70,7 +64,8 @@ def test_lloyd_objective_fp64(km, gpu, prec):
 
 @pytest.mark.parametrize("prec", PRECISIONS)
 @pytest.mark.parametrize("shape", [(1000, 1, 3), (129, 7, 129), (5000, 65, 100), (3333, 250, 17),
-                                   (2048, 130, 256), (10007, 12, 2)])
+                                   (2048, 130, 256), (10007, 12, 2), (20000, 64, 300), (8000, 200, 777),
+                                   (5000, 16, 2000), (6000, 256, 4096)])
 def test_assign_exact_vs_oracle(km, gpu, prec, shape):
     import torch
     n, d, k = shape
@@ -81,11 +76,6 @@ def test_assign_exact_vs_oracle(km, gpu, prec, shape):
     lab_o, md_o = helpers.orc_assign(X, Cc)
     Xt = torch.from_numpy(X).to(gpu)
     Ct = torch.from_numpy(Cc).to(gpu)
-    if prec == "bf16x3" and (d + 63) // 64 * 64 * k * 4 > 150 * 1024:
-        with pytest.raises(km.KmError) as e:
-            km.assign(Xt, Ct, precision=prec)
-        assert e.value.status == km.KM_ERR_UNSUPPORTED
-        return
     lab, md, refined = km.assign(Xt, Ct, precision=prec, want_mindist=True)
     np.testing.assert_array_equal(lab.cpu().numpy().astype(np.uint32), lab_o)
 
@@ -110,11 +100,13 @@ def test_assign_near_ties(km, gpu, prec):
 
 
 @pytest.mark.parametrize("prec", PRECISIONS)
-def test_distances_vs_torch_fp32(km, gpu, prec):
+@pytest.mark.parametrize("shape", [(3000, 96, 200), (2000, 64, 700)])
+def test_distances_vs_torch_fp32(km, gpu, prec, shape):
     """The fast-path distance stage against a plain PyTorch fp32 reference
-    (FP64 for the comparison); tolerance = the bound the refinement uses."""
+    (FP64 for the comparison); tolerance = the bound the refinement uses.
+    k = 700 runs the chunked tensor-core kernel."""
     import torch
-    n, d, k = 3000, 96, 200
+    n, d, k = shape
     rng = np.random.default_rng(3)
     X = torch.from_numpy(rng.standard_normal((n, d)).astype(np.float32) * 2).to(gpu)
     Cc = torch.from_numpy(rng.standard_normal((k, d)).astype(np.float32) * 2).to(gpu)
