@@ -318,6 +318,193 @@ def ours_arm(args, rank, world):
     return line
 
 
+# ---------------------------------------------------------------------------
+# Secondary workloads (--workload bigk | kkm): the very-large-k Lloyd case and
+# kernel k-means with a precomputed kernel matrix.  Same JSON contract, one GPU.
+# ---------------------------------------------------------------------------
+BIGK = dict(n=4_194_304, d=256, k=4096, lo=-20.0, hi=20.0, sigma_range=(0.2, 2.0), zipf=1.1, seed=5000,
+            tol=1e-5)
+KKM = dict(n=65_536, d=512, k=64, lo=-1.0, hi=1.0, sigma=0.25, seed=3000)
+
+
+def _event_ms(fn, stream):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    out = fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), out
+
+
+def bigk_arm(args):
+    """Lloyd with n = 4,194,304, d = 256, k = 4096, BF16-stored points from a
+    seeded mixture with Zipf(1.1) cluster sizes, per-cluster sigma U[0.2, 2],
+    centers U[-20, 20]^256.  BF16 tensor cores + exact refinement against the
+    FP32 plain path on the same points."""
+    import torch
+    import helpers
+    km = helpers.km()
+    c = BIGK
+    n, d, k = (args.rows or c["n"]), c["d"], c["k"]
+    stream = torch.cuda.Stream()
+    X = km.synth_blobs(n, d, k, c["lo"], c["hi"], 1.0, c["seed"], sigma_range=c["sigma_range"],
+                       zipf_s=c["zipf"], nthreads=os.cpu_count() or 8)
+    with torch.cuda.stream(stream):
+        bits = torch.from_numpy(X).cuda().to(torch.bfloat16).view(torch.int16)
+    torch.cuda.synchronize()
+    Xd = bits.view(torch.bfloat16).float()                 # the points as FP32 (exact)
+    steps32 = 2
+    res = {}
+    with torch.cuda.stream(stream):
+        for prec, steps in ((args.precision, args.steps), ("fp32", steps32)):
+            m = km.Lloyd(n, d, k, tol=c["tol"], seed=1, maxiter=steps, precision=prec, conv="none",
+                         stream=stream.cuda_stream).set_data_bf16(bits)
+            m.fit(want_centroids=False)                    # warm-up fit (builds the graph)
+            torch.cuda.synchronize()
+            clk = Clocks(0)
+            with clk:
+                lab, _, r = m.fit(want_centroids=False)
+            stages = m.profile(3) if prec != "fp32" else None
+            res[prec] = dict(ms=r.fit_ms, iters=r.iterations, launches=r.kernel_launches, clocks=clk.summary(),
+                             refined=r.refined_rows, full=r.full_rescore_rows, stages=stages)
+            m.close()
+        # label agreement after the same iterations from the same seeded start
+        m = km.Lloyd(n, d, k, tol=c["tol"], seed=1, maxiter=steps32, precision=args.precision, conv="none",
+                     stream=stream.cuda_stream).set_data_bf16(bits)
+        lab_b, _, _ = m.fit(want_centroids=False)
+        m.close()
+        m = km.Lloyd(n, d, k, tol=c["tol"], seed=1, maxiter=steps32, precision="fp32", conv="none",
+                     stream=stream.cuda_stream).set_data(Xd)
+        lab_f, _, _ = m.fit(want_centroids=False)
+        m.close()
+    agree = float((lab_b == lab_f).mean())
+    sizes = np.bincount(lab_b, minlength=k)
+    rb = res[args.precision]
+    value = rb["iters"] / (rb["ms"] / 1e3)
+    v32 = res["fp32"]["iters"] / (res["fp32"]["ms"] / 1e3)
+    hbm, bf16, src = peaks()
+    names = ["distance+argmin", "refine", "label sort", "centroid sums", "finalize+control"]
+    st = rb["stages"]
+    flops = 2.0 * n * k * d
+    ach = flops / (st[0] / 1e3) / 1e12
+    # e2e: BF16 bits from pinned host memory through the C ABI
+    hb = bits.cpu().pin_memory()
+    import ctypes as C
+    lab = torch.empty(n, dtype=torch.int32).pin_memory()
+    with torch.cuda.stream(stream):
+        m = km.Lloyd(n, d, k, tol=c["tol"], seed=1, maxiter=args.steps, precision=args.precision, conv="none",
+                     stream=stream.cuda_stream)
+        r = km.Result()
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            km.check(km.lib().km_lloyd_set_data_bf16(m.h, hb.data_ptr(), 0), "set_data_bf16")
+            km.check(km.lib().km_lloyd_fit(m.h, None, lab.data_ptr(), None, C.byref(r)), "fit")
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        m.close()
+    # CPU baseline: the oracle port on a row sample, scaled to n
+    threads = os.cpu_count() or 1
+    samp = 8192
+    Xs = Xd[:samp].cpu().numpy()
+    C0 = Xs[np.random.default_rng(0).choice(samp, k, replace=False)].copy()
+    t0 = time.perf_counter()
+    lab_s, _ = helpers.orc_assign(Xs, C0, threads=threads)
+    helpers.orc_update(Xs, lab_s, k, threads=threads)
+    secs = time.perf_counter() - t0
+    cpu_v = 1.0 / (secs * n / samp)
+    return {
+        "metric": "iters/s (n=4M,d=256,k=4096, BF16 points): BF16-TC vs FP32 plain at equal labels",
+        "value": value, "unit": "iters/s", "n_gpus": 1, "steps": args.steps, "warmup": args.steps,
+        "ms_per_step": rb["ms"] / rb["iters"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": f"lloyd n={n} d=256 k=4096, BF16-stored points, Zipf(1.1) sizes, "
+                               "sigma U[0.2,2], centers U[-20,20]", "n": n, "d": d, "k": k,
+                   "l2": "inputs larger than L2 (BF16 X 2 GiB)", "parallelism": "single GPU"},
+        "precision": args.precision,
+        "fp32_plain": {"value": v32, "unit": "iters/s", "iters": res["fp32"]["iters"]},
+        "speedup_vs_fp32_plain": value / v32,
+        "label_agreement_vs_fp32": agree,
+        "refined_rows_per_iter": rb["refined"] / max(1, rb["iters"]),
+        "full_rescore_rows_per_iter": rb["full"] / max(1, rb["iters"]),
+        "cluster_sizes": {"max": int(sizes.max()), "median": float(np.median(sizes)), "empty": int((sizes == 0).sum())},
+        "stages_ms": dict(zip(names, st)),
+        "roofline": {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16,
+                     "kernel": "distance+argmin (assign_tc_chunked_kernel)", "ms": st[0], "peak_source": src,
+                     "traffic": None},
+        "e2e": {"value": r.iterations / wall, "unit": "iters/s", "h2d_bytes_per_step": n * d * 2,
+                "d2h_bytes_per_step": n * 4,
+                "step": f"km_lloyd_set_data_bf16 from pinned host + seeded init + {r.iterations} iterations + "
+                        f"labels D2H; wall {wall * 1e3:.1f} ms"},
+        "cpu_baseline": {"value": cpu_v, "unit": "iters/s", "cores": threads, "kind": "port",
+                         "sample": f"one assignment+update of {samp} rows against k={k} (oracle port), "
+                                   f"{secs:.2f} s, scaled by n/{samp}"},
+        "clocks": rb["clocks"],
+        "gpu_launches": rb["launches"],
+    }
+
+
+def kkm_arm(args):
+    """Kernel k-means with a precomputed kernel matrix: n = 65,536, d = 512,
+    k = 64, 64 seeded blobs (centers U[-1,1]^512, sigma 0.25); polynomial
+    (x.y/d + 1)^2 and Gaussian (sigma 0.5) kernels; K stored FP32 (16 GiB)
+    or BF16 (8 GiB); K built on the tensor cores (split-BF16x3 for FP32
+    storage, BF16 for BF16 storage)."""
+    import torch
+    import helpers
+    km = helpers.km()
+    c = KKM
+    n, d, k = c["n"], c["d"], c["k"]
+    X = km.synth_blobs(n, d, k, c["lo"], c["hi"], c["sigma"], c["seed"], nthreads=os.cpu_count() or 8)
+    Xd = torch.from_numpy(X).cuda()
+    stream = torch.cuda.current_stream()
+    hbm, bf16, src = peaks()
+    rows = {}
+    for kern, params in (("polynomial", dict(gamma=1.0 / d, coef=1.0, degree=2)), ("gaussian", dict(sigma=0.5))):
+        for kb16 in (False, True):
+            prec = "bf16" if kb16 else "bf16x3"
+            # K build alone (tensor cores, kernel function fused in the epilogue)
+            kb_ms = []
+            for _ in range(2):
+                ms, K = _event_ms(lambda: km.kernel_matrix(Xd, kernel=kern, precision=prec, out_bf16=kb16,
+                                                           **params), stream)
+                kb_ms.append(ms)
+                del K
+            torch.cuda.empty_cache()
+            m = km.KernelKMeans(n, d, k, kernel=kern, maxiter=args.steps, precision=prec, k_bf16=kb16,
+                                **params).set_data(Xd)
+            m.fit()                                        # warm-up
+            clk = Clocks(0)
+            with clk:
+                lab, r = m.fit()
+            m.close()
+            torch.cuda.empty_cache()
+            ips = r.iterations / (r.fit_ms / 1e3)
+            kbytes = n * n * (2 if kb16 else 4)
+            it_ms = r.fit_ms / r.iterations
+            rows[f"{kern}/{'bf16' if kb16 else 'fp32'}K"] = {
+                "iters_per_s": ips, "ms_per_iter": it_ms, "k_build_ms": min(kb_ms),
+                "k_build_tflops": 2.0 * n * n * d / (min(kb_ms) / 1e3) / 1e12,
+                "iter_gbs": (kbytes + 4 * n + 4 * n * k) / (it_ms / 1e3) / 1e9,
+                "score": r.score, "clocks": clk.summary(), "launches": r.kernel_launches}
+    head = rows["polynomial/fp32K"]
+    return {
+        "metric": "iters/s (kernel k-means n=65536,d=512,k=64, precomputed K)",
+        "value": head["iters_per_s"], "unit": "iters/s", "n_gpus": 1, "steps": args.steps, "warmup": args.steps,
+        "ms_per_step": head["ms_per_iter"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "kernel k-means n=65536 d=512 k=64, polynomial (x.y/d+1)^2, K FP32 16 GiB",
+                   "n": n, "d": d, "k": k, "l2": "K larger than L2", "parallelism": "single GPU"},
+        "variants": rows,
+        "roofline": {"bound": "hbm", "achieved": head["iter_gbs"], "peak": hbm, "unit": "GB/s",
+                     "frac": head["iter_gbs"] / hbm, "kernel": "kkm_vk_kernel (V.K streaming of K)",
+                     "peak_source": src, "traffic": None},
+        "clocks": head["clocks"], "gpu_launches": head["launches"],
+    }
+
+
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the stage's
 # dominant kernel, from one ncu capture of this command
 # (profiles/lloyd_iteration_n1M_d128_k256_launches.md; averages over the
@@ -340,6 +527,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "bf16x3", "fp32"])
+    ap.add_argument("--workload", default="lloyd", choices=["lloyd", "bigk", "kkm"],
+                    help="lloyd: the headline n=1M d=128 k=256 workload (default); bigk: n=4M d=256 "
+                         "k=4096 BF16 points; kkm: kernel k-means n=65536 d=512 k=64")
+    ap.add_argument("--rows", type=int, default=0,
+                    help="bigk only: fewer rows than the workload's n (a smaller case for profilers)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -347,6 +539,11 @@ def main():
     if args.impl == "reference":
         line = reference_arm(args, rank)
         if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if args.workload != "lloyd":
+        if rank == 0:
+            line = bigk_arm(args) if args.workload == "bigk" else kkm_arm(args)
             print(json.dumps(line), flush=True)
         return
     if world > 1:

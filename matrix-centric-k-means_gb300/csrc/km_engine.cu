@@ -44,7 +44,7 @@ void set_last_error(cudaError_t e, const char* what, const char* file, int line)
 const char* last_error_text() { return g_last_error.c_str(); }
 
 // Relative error coefficients of the fast distance path (see TieBound).
-TieBound make_tie_bound(int precision, uint32_t d) {
+TieBound make_tie_bound(int precision, uint32_t d, bool a_exact) {
   const double u = std::ldexp(1.0, -24);
   const double ub = std::ldexp(1.0, -8);
   const double uacc = std::ldexp(1.0, -22);  // tensor-core FP32 accumulation, 4 ulp per add
@@ -53,7 +53,13 @@ TieBound make_tie_bound(int precision, uint32_t d) {
   if (precision == KM_PREC_FP32) {
     eps = gamma((double)d, u);
   } else if (precision == KM_PREC_BF16) {
-    eps = 2 * ub + ub * ub + (1 + ub) * (1 + ub) * gamma((double)d, uacc);
+    // |x^ c^ - x c| <= (2ub + ub^2) |x||c| per term (ub only when x^ = x),
+    // plus FP32 accumulation of d products
+    eps = a_exact ? ub + (1 + ub) * gamma((double)d, uacc)
+                  : 2 * ub + ub * ub + (1 + ub) * (1 + ub) * gamma((double)d, uacc);
+  } else if (a_exact) {
+    // split-2: c = c_hi + c_lo + r, |r| <= ub^2 |c|; 2d exact products accumulated
+    eps = ub * ub + (1 + 2 * ub) * gamma(2.0 * d, uacc);
   } else {
     eps = 3.5 * ub * ub + (1 + 5 * ub) * gamma(3.0 * d, uacc);
   }
@@ -70,7 +76,8 @@ LloydEngine::~LloydEngine() {
   dfree(X_owned); dfree(xn2); dfree(xn2d); dfree(Xb); dfree(Xlo);
   dfree(C); dfree(Cn); dfree(cn2); dfree(dsq); dfree(objpart); dfree(shift_c); dfree(obj_c);
   dfree(Cb); dfree(Clo); dfree(labels); dfree(mindist); dfree(queue); dfree(qfull); dfree(Ct);
-  dfree(qcnt); dfree(qfcnt);
+  dfree(qcnt); dfree(qfcnt); dfree(qwide); dfree(qwcnt); dfree(wlc); dfree(wl);
+  dfree(q2); dfree(q2full); dfree(q2cnt); dfree(q2fcnt); dfree(fidx); dfree(nfull);
   dfree(seghist); dfree(counts); dfree(cstart); dfree(perm); dfree(red_part); dfree(st);
   if (h_st) cudaFreeHost(h_st);
   if (own_stream && stream) cudaStreamDestroy(stream);
@@ -100,16 +107,21 @@ km_status LloydEngine::init(uint64_t n_, uint32_t d_, uint32_t k_, int precision
   dp = round_up(d, 64);
   kp = round_up(std::max<uint32_t>(k, 16), 16);
   if (precision != KM_PREC_FP32) {
-    if (kp <= 256) tc = plan_tc(dp, kp, precision == KM_PREC_BF16X3, n, num_sms);
+    // planned for the widest operands of the precision; SPLIT2 (chosen at
+    // set_points when the points turn out to be exact BF16) needs less
+    const int plan_mode = precision == KM_PREC_BF16X3 ? TC_SPLIT3 : TC_PLAIN;
+    if (kp <= 256) tc = plan_tc(dp, kp, plan_mode, n, num_sms);
     if (!tc.ok) {
       // k > 256, or the centroid operand does not fit shared memory whole
-      tc = plan_tc_chunked(dp, k, precision == KM_PREC_BF16X3, n, num_sms);
+      tc = plan_tc_chunked(dp, k, plan_mode, n, num_sms);
       if (tc.ok) kp = tc.kp;            // centroid operand padded to whole chunks
     }
     if (!tc.ok) return KM_ERR_UNSUPPORTED;
-    KM_TRY(tc_set_attributes(tc, precision == KM_PREC_BF16X3));
+    KM_TRY(tc_set_attributes(tc, plan_mode));
+    if (plan_mode == TC_SPLIT3) KM_TRY(tc_set_attributes(tc, TC_SPLIT2));
+    tc_mode = plan_mode;
   }
-  tb = make_tie_bound(precision, d);
+  tb = make_tie_bound(precision, d, false);
 
   KM_TRY(dalloc(&xn2, n));
   KM_TRY(dalloc(&xn2d, n));
@@ -132,6 +144,25 @@ km_status LloydEngine::init(uint64_t n_, uint32_t d_, uint32_t k_, int precision
     KM_TRY(dalloc(&qcnt, rows / 32));
     KM_TRY(dalloc(&qfcnt, rows / 32));
     rq = RefineQueues{queue, qfull, qcnt, qfcnt, rows / 32};
+    if (precision != KM_PREC_FP32 && tc.chunked) {
+      // candidate lists of the chunked distance kernel: up to 256 per row,
+      // fewer when the lists would pass 16 GiB
+      uint32_t L = 256;
+      while (L > 32 && (uint64_t)rows * L * sizeof(uint2) > (16ull << 30)) L -= 32;
+      KM_TRY(dalloc(&qwide, rows));
+      KM_TRY(dalloc(&qwcnt, rows / 32));
+      KM_TRY(dalloc(&wlc, rows));
+      KM_TRY(dalloc(&wl, (size_t)rows * L));
+      rq.wide = qwide; rq.wcnt = qwcnt; rq.wl = wl; rq.wlc = wlc; rq.L = L;
+      KM_TRY(dalloc(&q2, rows));
+      KM_TRY(dalloc(&q2full, rows));
+      KM_TRY(dalloc(&q2cnt, rows / 32));
+      KM_TRY(dalloc(&q2fcnt, rows / 32));
+      KM_TRY(dalloc(&fidx, rows));
+      KM_TRY(dalloc(&nfull, 1));
+      rq2 = RefineQueues{q2, q2full, q2cnt, q2fcnt, rows / 32};
+      tb32 = make_tie_bound(KM_PREC_FP32, d, false);
+    }
   }
   KM_TRY(dalloc(&Ct, (size_t)k * d));
   KM_TRY(dalloc(&red_part, 256));
@@ -183,6 +214,7 @@ km_status LloydEngine::set_points(const float* Xsrc, bool on_device, bool copy) 
   }
   refine_v4 = (d % 4 == 0) && (reinterpret_cast<uintptr_t>(X) % 16 == 0);
   KM_CUDA_TRY(cudaMemsetAsync(&st->err, 0, sizeof(uint32_t), stream));
+  KM_CUDA_TRY(cudaMemsetAsync(&st->x_not_bf16, 0, sizeof(uint32_t), stream));
   const int blocks = (int)std::min<uint64_t>((n + 7) / 8, (uint64_t)num_sms * 16);
   prep_points_kernel<<<blocks, 256, 0, stream>>>(X, n, d, dp, xn2, xn2d, Xb, Xlo, st);
   KM_CUDA_TRY(cudaGetLastError());
@@ -203,6 +235,9 @@ km_status LloydEngine::set_points(const float* Xsrc, bool on_device, bool copy) 
   }
   KM_TRY(read_state());
   if (h_st->err & KM_DEVERR_NONFINITE) return KM_ERR_ARG;
+  a_exact = h_st->x_not_bf16 == 0u;
+  tb = make_tie_bound(precision, d, a_exact);
+  if (precision == KM_PREC_BF16X3) tc_mode = a_exact ? TC_SPLIT2 : TC_SPLIT3;
   data_ready = true;
   return KM_OK;
 }
@@ -265,13 +300,16 @@ km_status LloydEngine::enqueue_distance(float* Dout) {
   if (precision == KM_PREC_FP32) {
     KM_TRY(launch_assign_f32(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist, rq, Dout, stream));
   } else {
-    KM_TRY(launch_assign_tc(tc, precision == KM_PREC_BF16X3, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k,
+    KM_TRY(launch_assign_tc(tc, tc_mode, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k,
                             kp, tb, st, labels, mindist, rq, Dout, stream));
   }
   return KM_OK;
 }
 
 km_status LloydEngine::enqueue_refine() {
+  if (rq.wide)
+    return launch_refine_gemm(refine_v4, num_sms, X, C, Ct, cn2, xn2, n, d, k, tb32, st, rq, rq2, fidx,
+                              nfull, labels, mindist, stream);
   return launch_refine(refine_v4, num_sms, X, C, Ct, d, k, st, rq, labels, mindist, stream);
 }
 

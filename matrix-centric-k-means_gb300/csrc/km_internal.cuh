@@ -41,7 +41,7 @@ struct DevState {
   uint32_t iter;            // iterations executed
   uint32_t converged_iter;  // iteration at which the stop rule fired (0: not yet)
   uint32_t moved;           // some centroid moved more than tol in this iteration
-  uint32_t pad2;
+  uint32_t x_not_bf16;      // set_data: some coordinate is not exactly a BF16 value
   uint32_t err;             // device error bits (KM_DEVERR_*)
   uint32_t err_where;       // first wait that ran out (diagnostics)
   uint32_t pad3;
@@ -91,7 +91,9 @@ struct TieBound {
   float safety; // multiplier on the right-hand side (covers this test's own rounding)
 };
 
-TieBound make_tie_bound(int precision, uint32_t d);
+// a_exact: every point coordinate is exactly a BF16 value, so only the
+// centroid operand carries a rounding error.
+TieBound make_tie_bound(int precision, uint32_t d, bool a_exact);
 
 __device__ __forceinline__ int tie_class(float X2, float v1, float v2, float v3, float cn1,
                                          float cmax, const TieBound& tb) {
@@ -173,6 +175,12 @@ struct RefineQueues {
   uint32_t* ccnt;      // per 32-row segment: entries in cand
   uint32_t* fcnt;      // per 32-row segment: entries in full
   uint64_t nseg;       // segments (rows rounded up to whole 128-row tiles, / 32)
+  // chunked distance kernel only (null otherwise): rows with 5..L candidates
+  uint32_t* wide;      // row ids, segmented like full
+  uint32_t* wcnt;      // per segment: entries in wide
+  uint2* wl;           // per row: L (centroid, value bits) pairs, candidates first (L <= 256)
+  uint32_t* wlc;       // per row: candidates in wl (valid for rows in wide)
+  uint32_t L;
 };
 
 // Refinement queues are segmented by rows: the 32 rows r with r >> 5 == seg own

@@ -23,6 +23,14 @@ km_status launch_assign_f32(const float* X, const float* C, const float* cn2, co
 km_status launch_refine(bool v4, int num_sms, const float* X, const float* C, const float* Ct,
                         uint32_t d, uint32_t k, DevState* st, const RefineQueues& rq,
                         uint32_t* labels, float* mindist, cudaStream_t s);
+// Chunked-kernel refinement: candidate and wide queues as launch_refine; rows
+// of the full queue go through the FP32 distance kernel on those rows alone
+// (gathered by index into fidx) and then the exact re-score of its near ties.
+km_status launch_refine_gemm(bool v4, int num_sms, const float* X, const float* C, const float* Ct,
+                             const float* cn2, const float* xn2, uint64_t n, uint32_t d, uint32_t k,
+                             TieBound tb32, DevState* st, const RefineQueues& rq,
+                             const RefineQueues& rq2, uint32_t* fidx, uint32_t* nfull,
+                             uint32_t* labels, float* mindist, cudaStream_t s);
 __global__ void seg_hist_kernel(const uint32_t* labels, uint64_t n, uint32_t k, uint32_t seg,
                                 uint32_t nseg, uint32_t* seghist, DevState* st);
 __global__ void seg_scan_kernel(uint32_t* seghist, uint32_t k, uint32_t nseg, uint32_t* counts,
@@ -53,12 +61,16 @@ struct TcPlan {
   size_t smem = 0;       // dynamic shared memory bytes
   int grid = 0;
 };
-TcPlan plan_tc(uint32_t dp, uint32_t kp, bool x3, uint64_t n, int num_sms);
-TcPlan plan_tc_chunked(uint32_t dp, uint32_t k, bool x3, uint64_t n, int num_sms);
+// Operand modes of the tensor-core distance kernels.  PLAIN: BF16 x BF16.
+// SPLIT3: x = hi + lo and c = hi + lo, hi*hi + hi*lo + lo*hi.  SPLIT2: the
+// points are exact in BF16 (lo = 0), so hi*hi + hi*lo_c alone.
+enum : int { TC_PLAIN = 0, TC_SPLIT3 = 1, TC_SPLIT2 = 2 };
+TcPlan plan_tc(uint32_t dp, uint32_t kp, int mode, uint64_t n, int num_sms);
+TcPlan plan_tc_chunked(uint32_t dp, uint32_t k, int mode, uint64_t n, int num_sms);
 km_status encode_tmap_bf16(CUtensorMap* tm, const void* base, uint64_t inner, uint64_t outer,
                            uint32_t box_inner, uint32_t box_outer);
-km_status tc_set_attributes(const TcPlan& pl, bool x3);
-km_status launch_assign_tc(const TcPlan& pl, bool x3, const CUtensorMap& tmA,
+km_status tc_set_attributes(const TcPlan& pl, int mode);
+km_status launch_assign_tc(const TcPlan& pl, int mode, const CUtensorMap& tmA,
                            const CUtensorMap& tmAlo, const CUtensorMap& tmB,
                            const CUtensorMap& tmBlo, const float* cn2, const float* xn2,
                            uint64_t n, uint32_t k, uint32_t kp, TieBound tb, DevState* st,
@@ -114,8 +126,18 @@ struct LloydEngine {
   uint32_t seg = 1024, nseg = 0;
   int sort_wpb = 8;
   size_t sort_smem = 0;
+  RefineQueues rq2{};           // chunked kernel: queues of the FP32 pass over full rows
+  RefineEntry* q2 = nullptr;
+  uint32_t *q2full = nullptr, *q2cnt = nullptr, *q2fcnt = nullptr, *fidx = nullptr, *nfull = nullptr;
+  TieBound tb32{};
+  uint32_t* qwide = nullptr;   // chunked kernel: rows with 5..32 candidates
+  uint32_t* qwcnt = nullptr;
+  uint32_t* wlc = nullptr;
+  uint2* wl = nullptr;
   TieBound tb{};
   TcPlan tc{};
+  int tc_mode = 0;          // TC_PLAIN / TC_SPLIT3 / TC_SPLIT2
+  bool a_exact = false;     // every point coordinate is a BF16 value
   CUtensorMap tmA{}, tmAlo{}, tmB{}, tmBlo{};
   bool data_ready = false;
 

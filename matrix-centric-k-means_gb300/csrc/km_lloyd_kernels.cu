@@ -37,10 +37,11 @@ __global__ void prep_points_kernel(const float* __restrict__ X, uint64_t n, uint
   for (uint64_t r = warp; r < n; r += nw) {
     const float* x = X + r * d;
     double s = 0.0;
-    bool bad = false;
+    bool bad = false, inexact = false;
     for (uint32_t j = lane; j < dp; j += 32) {
       float v = (j < d) ? x[j] : 0.0f;
       if (!isfinite(v)) bad = true;
+      if ((__float_as_uint(v) & 0xffffu) != 0u) inexact = true;    // not a BF16 value
       s += (double)v * (double)v;
       if (Xb) {
         __nv_bfloat16 hi = __float2bfloat16_rn(v);
@@ -50,6 +51,7 @@ __global__ void prep_points_kernel(const float* __restrict__ X, uint64_t n, uint
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&st->err, KM_DEVERR_NONFINITE);
+    if (__any_sync(0xffffffffu, inexact) && lane == 0) atomicOr(&st->x_not_bf16, 1u);
     if (lane == 0) {
       xn2[r] = (float)s;
       if (xn2d) xn2d[r] = s;
@@ -131,8 +133,14 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
                   const float* __restrict__ cn2, const float* __restrict__ xn2, uint64_t n,
                   uint32_t d, uint32_t k, TieBound tb, DevState* st,
                   uint32_t* __restrict__ labels, float* __restrict__ mindist,
-                  RefineQueues rq, float* __restrict__ Dout) {
+                  RefineQueues rq, float* __restrict__ Dout, const uint32_t* __restrict__ ridx,
+                  const uint32_t* __restrict__ nidx) {
   if (st->done) return;
+  // Gather mode (ridx != null): logical row li of the tiles is row ridx[li] of X,
+  // for li < *nidx; queue segments are taken over the logical rows.
+  const uint64_t n_log = ridx ? (uint64_t)*nidx : n;
+  if ((uint64_t)blockIdx.x * SM_ >= n_log) return;
+  __shared__ uint32_t rmap[SM_];
   __shared__ __align__(16) float As[2][SK_][SM_ + SPAD];
   __shared__ __align__(16) float Bs[2][SK_][SN_ + SPAD];
   __shared__ float cns[SN_];
@@ -144,7 +152,10 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
   if (tid < SM_) {
     bv1[tid] = bv2[tid] = bv3[tid] = f_inf();
     bi1[tid] = bi2[tid] = 0xffffffffu;
+    const uint64_t li = m0 + tid;
+    rmap[tid] = ridx ? (li < n_log ? ridx[li] : 0u) : (uint32_t)li;
   }
+  __syncthreads();
   const uint32_t ntiles = (k + SN_ - 1) / SN_;
   const uint32_t nk = (d + SK_ - 1) / SK_;
 
@@ -167,10 +178,11 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
           const int idx = e * 256 + tid;
           const int r = idx >> 2, c4 = idx & 3;
           const uint32_t col = kc + 4u * (uint32_t)c4;
-          const uint64_t row = m0 + r;
+          const bool rv = m0 + r < n_log;
+          const uint64_t row = rmap[r];
           const uint32_t cc = c0 + r;
           float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-          if (row < n && col < d) a = __ldg(reinterpret_cast<const float4*>(X + row * d + col));
+          if (rv && col < d) a = __ldg(reinterpret_cast<const float4*>(X + row * d + col));
           if (cc < k && col < d) b = __ldg(reinterpret_cast<const float4*>(C + (uint64_t)cc * d + col));
           ra[4 * e + 0] = a.x; ra[4 * e + 1] = a.y; ra[4 * e + 2] = a.z; ra[4 * e + 3] = a.w;
           rb[4 * e + 0] = b.x; rb[4 * e + 1] = b.y; rb[4 * e + 2] = b.z; rb[4 * e + 3] = b.w;
@@ -181,8 +193,8 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
           const int idx = e * 256 + tid;
           const int r = idx >> 4, kk = idx & 15;
           const uint32_t col = kc + kk;
-          const uint64_t row = m0 + r;
-          ra[e] = (row < n && col < d) ? X[row * d + col] : 0.0f;
+          const uint64_t row = rmap[r];
+          ra[e] = (m0 + r < n_log && col < d) ? X[row * d + col] : 0.0f;
           const uint32_t cc = c0 + r;
           rb[e] = (cc < k && col < d) ? C[(uint64_t)cc * d + col] : 0.0f;
         }
@@ -237,7 +249,7 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int r = ty * 8 + i;
-      const uint64_t row = m0 + r;
+      const uint64_t row = m0 + r;                      // Dout is written in direct mode only
       Top3 t;
       t.init();
 #pragma unroll
@@ -263,8 +275,9 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
 
   // Classify rows (one thread per row) and queue near ties.
   if (tid < SM_) {
-    const uint64_t row = m0 + tid;
-    const bool valid = row < n;
+    const uint64_t li = m0 + tid;
+    const bool valid = li < n_log;
+    const uint64_t row = rmap[tid];
     int cls = 0;
     uint32_t i1 = bi1[tid] == 0xffffffffu ? 0u : bi1[tid];
     if (valid) {
@@ -274,7 +287,7 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
       if (mindist) mindist[row] = bv1[tid] + xn2[row];
     }
     RefineEntry e{(uint32_t)row, 2u, {i1, bi2[tid], 0u, 0u}};
-    const uint64_t seg = row >> 5;
+    const uint64_t seg = li >> 5;
     seg_push(rq.cand, rq.ccnt, seg, valid && cls == 1, e);
     seg_push(rq.full, rq.fcnt, seg, valid && cls == 2, (uint32_t)row);
   }
@@ -289,10 +302,10 @@ km_status launch_assign_f32(const float* X, const float* C, const float* cn2, co
                   (reinterpret_cast<uintptr_t>(C) % 16 == 0);
   if (v4)
     assign_f32_kernel<true><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
-                                                   rq, Dout);
+                                                   rq, Dout, nullptr, nullptr);
   else
     assign_f32_kernel<false><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
-                                                    rq, Dout);
+                                                    rq, Dout, nullptr, nullptr);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }
@@ -322,7 +335,7 @@ template <bool V4>
 __global__ void __launch_bounds__(256)
 refine_cands_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
                     DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
-                    float* __restrict__ mindist) {
+                    float* __restrict__ mindist, bool count) {
   if (st->done) return;
   const int lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -360,65 +373,113 @@ refine_cands_kernel(const float* __restrict__ X, const float* __restrict__ C, ui
       }
     }
   }
-  if (lane == 0 && done_rows) atomicAdd(&st->refined_total, (unsigned long long)done_rows);
+  if (count && lane == 0 && done_rows) atomicAdd(&st->refined_total, (unsigned long long)done_rows);
 }
 
-// Exact re-score against all k centroids: one warp per row, lanes over
-// centroids (eight chains per lane), centroids read from the transposed copy
-// Ct (d x k) so that every load of the warp is one coalesced 128-byte line.
+// Exact re-score against all k centroids: one warp per group of up to four
+// rows of a segment, lanes over centroids (eight chains per lane and row),
+// centroids read from the transposed copy Ct (d x k) so that every load of
+// the warp is one coalesced 128-byte line and serves all rows of the group.
 // Per lane the centroids are visited in ascending order with a strict '<'
 // and the warp reduction keeps the lowest index on ties: the reference's
 // argmin (kmeans.cpp:106-122).
+constexpr int FULL_ROWS = 4;
+
 __global__ void __launch_bounds__(256)
 refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, uint32_t d, uint32_t k,
                    DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
-                   float* __restrict__ mindist) {
+                   float* __restrict__ mindist, bool count) {
   if (st->done) return;
   const int lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  // Work items: (segment, entry) pairs, one warp each; segments are walked in
-  // warp-strided order and each of their entries handed out in turn.
   uint32_t done_rows = 0;
   for (uint64_t seg = warp; seg < rq.nseg; seg += nw) {
    const uint32_t cnt = rq.fcnt[seg];
    done_rows += cnt;
-   for (uint32_t e = 0; e < cnt; ++e) {
-    const uint32_t row = rq.full[seg * 32 + e];
-    const float* x = X + (uint64_t)row * d;
-    float bv = f_inf();
-    uint32_t bi = 0xffffffffu;
-    for (uint32_t cb = 0; cb < k; cb += 256) {
-      float s[8];
+   for (uint32_t e0 = 0; e0 < cnt; e0 += FULL_ROWS) {
+    const uint32_t nr = min(cnt - e0, (uint32_t)FULL_ROWS);
+    uint32_t row[FULL_ROWS];
+    const float* x[FULL_ROWS];
 #pragma unroll
-      for (int t = 0; t < 8; ++t) s[t] = 0.0f;
+    for (int r = 0; r < FULL_ROWS; ++r) {
+      row[r] = rq.full[seg * 32 + e0 + min((uint32_t)r, nr - 1)];   // pad with the last row
+      x[r] = X + (uint64_t)row[r] * d;
+    }
+    float bv[FULL_ROWS];
+    uint32_t bi[FULL_ROWS];
+#pragma unroll
+    for (int r = 0; r < FULL_ROWS; ++r) { bv[r] = f_inf(); bi[r] = 0xffffffffu; }
+    for (uint32_t cb = 0; cb < k; cb += 256) {
+      float s[FULL_ROWS][8];
+#pragma unroll
+      for (int r = 0; r < FULL_ROWS; ++r)
+#pragma unroll
+        for (int t = 0; t < 8; ++t) s[r][t] = 0.0f;
       for (uint32_t j = 0; j < d; ++j) {
-        const float xj = x[j];
+        float xj[FULL_ROWS];
+#pragma unroll
+        for (int r = 0; r < FULL_ROWS; ++r) xj[r] = x[r][j];
         const float* ct = Ct + (uint64_t)j * k + cb + lane;
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
           if (cb + lane + 32 * t < k) {
-            const float tt = __fsub_rn(xj, ct[32 * t]);
-            s[t] = __fadd_rn(s[t], __fmul_rn(tt, tt));
+            const float cv = ct[32 * t];
+#pragma unroll
+            for (int r = 0; r < FULL_ROWS; ++r) {
+              const float tt = __fsub_rn(xj[r], cv);
+              s[r][t] = __fadd_rn(s[r][t], __fmul_rn(tt, tt));
+            }
           }
         }
       }
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
         const uint32_t c = cb + lane + 32 * t;
-        if (c < k && s[t] < bv) { bv = s[t]; bi = c; }
+#pragma unroll
+        for (int r = 0; r < FULL_ROWS; ++r)
+          if (c < k && s[r][t] < bv[r]) { bv[r] = s[r][t]; bi[r] = c; }
       }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-      const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-    }
-    if (lane == 0) {
-      labels[row] = (bi == 0xffffffffu) ? 0u : bi;
-      if (mindist) mindist[row] = bv;
+#pragma unroll
+    for (int r = 0; r < FULL_ROWS; ++r) {
+      float v = bv[r];
+      uint32_t i = bi[r];
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const uint32_t oi = __shfl_xor_sync(0xffffffffu, i, o);
+        if (ov < v || (ov == v && oi < i)) { v = ov; i = oi; }
+      }
+      if (lane == 0 && (uint32_t)r < nr) {
+        labels[row[r]] = (i == 0xffffffffu) ? 0u : i;
+        if (mindist) mindist[row[r]] = v;
+      }
     }
    }
+  }
+  if (count && lane == 0 && done_rows) {
+    atomicAdd(&st->refined_total, (unsigned long long)done_rows);
+    atomicAdd(&st->full_total, (unsigned long long)done_rows);
+  }
+}
+
+// Rows of the full queue gathered into one list (order irrelevant: every row
+// is re-scored on its own), counted as fully re-scored rows.
+__global__ void full_compact_kernel(DevState* st, RefineQueues rq, uint32_t* __restrict__ out,
+                                    uint32_t* __restrict__ nout) {
+  if (st->done) return;
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint32_t done_rows = 0;
+  for (uint64_t seg = warp; seg < rq.nseg; seg += nw) {
+    const uint32_t cnt = rq.fcnt[seg];
+    if (cnt == 0u) continue;
+    done_rows += cnt;
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(nout, cnt);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if ((uint32_t)lane < cnt) out[base + lane] = rq.full[seg * 32 + lane];
   }
   if (lane == 0 && done_rows) {
     atomicAdd(&st->refined_total, (unsigned long long)done_rows);
@@ -426,14 +487,102 @@ refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, ui
   }
 }
 
+// Exact re-score of rows with 5..L candidates (chunked distance kernel): one
+// warp per row, lanes stride over the row's candidates, the reference's CPU
+// distance; smallest distance wins, lowest index on ties.
+template <bool V4>
+__global__ void __launch_bounds__(256)
+refine_wide_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
+                   DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
+                   float* __restrict__ mindist) {
+  if (st->done) return;
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint32_t done_rows = 0;
+  for (uint64_t seg = warp; seg < rq.nseg; seg += nw) {
+    const uint32_t cnt = rq.wcnt[seg];
+    done_rows += cnt;
+    for (uint32_t e = 0; e < cnt; ++e) {
+      const uint32_t row = rq.wide[seg * 32 + e];
+      const uint32_t nc = min(rq.wlc[row], rq.L);
+      float bv = f_inf();
+      uint32_t bi = 0xffffffffu;
+      const float* x = X + (uint64_t)row * d;
+      for (uint32_t e = (uint32_t)lane; e < nc; e += 32u) {
+        const uint32_t c = rq.wl[(uint64_t)row * rq.L + e].x;
+        const float* cc = C + (uint64_t)c * d;
+        const float v = V4 ? cpu_dist_v4(x, cc, d) : cpu_dist(x, cc, d);
+        if (v < bv || (v == bv && c < bi)) { bv = v; bi = c; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+      }
+      if (lane == 0) {
+        labels[row] = (bi == 0xffffffffu) ? 0u : bi;
+        if (mindist) mindist[row] = bv;
+      }
+    }
+  }
+  if (lane == 0 && done_rows) atomicAdd(&st->refined_total, (unsigned long long)done_rows);
+}
+
 km_status launch_refine(bool v4, int num_sms, const float* X, const float* C, const float* Ct,
                         uint32_t d, uint32_t k, DevState* st, const RefineQueues& rq,
                         uint32_t* labels, float* mindist, cudaStream_t s) {
   if (v4)
-    refine_cands_kernel<true><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
+    refine_cands_kernel<true><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist, true);
   else
-    refine_cands_kernel<false><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
-  refine_full_kernel<<<num_sms * 4, 256, 0, s>>>(X, Ct, d, k, st, rq, labels, mindist);
+    refine_cands_kernel<false><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist, true);
+  if (rq.wide) {
+    if (v4)
+      refine_wide_kernel<true><<<num_sms * 8, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
+    else
+      refine_wide_kernel<false><<<num_sms * 8, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
+  }
+  refine_full_kernel<<<num_sms * 4, 256, 0, s>>>(X, Ct, d, k, st, rq, labels, mindist, true);
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
+
+km_status launch_refine_gemm(bool v4, int num_sms, const float* X, const float* C, const float* Ct,
+                             const float* cn2, const float* xn2, uint64_t n, uint32_t d, uint32_t k,
+                             TieBound tb32, DevState* st, const RefineQueues& rq,
+                             const RefineQueues& rq2, uint32_t* fidx, uint32_t* nfull,
+                             uint32_t* labels, float* mindist, cudaStream_t s) {
+  if (v4)
+    refine_cands_kernel<true><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist, true);
+  else
+    refine_cands_kernel<false><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist, true);
+  if (rq.wide) {
+    if (v4)
+      refine_wide_kernel<true><<<num_sms * 8, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
+    else
+      refine_wide_kernel<false><<<num_sms * 8, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
+  }
+  // rows of the full queue: FP32 distance pass over all k on those rows alone,
+  // then the exact re-score of its own near ties
+  KM_CUDA_TRY(cudaMemsetAsync(nfull, 0, sizeof(uint32_t), s));
+  // the gather pass writes the counts of the segments its rows reach only:
+  // every other segment of rq2 must read as empty
+  KM_CUDA_TRY(cudaMemsetAsync(rq2.ccnt, 0, sizeof(uint32_t) * rq2.nseg, s));
+  KM_CUDA_TRY(cudaMemsetAsync(rq2.fcnt, 0, sizeof(uint32_t) * rq2.nseg, s));
+  full_compact_kernel<<<num_sms * 4, 256, 0, s>>>(st, rq, fidx, nfull);
+  const unsigned blocks = (unsigned)((n + SM_ - 1) / SM_);
+  const bool gv4 = v4 && (reinterpret_cast<uintptr_t>(C) % 16 == 0);
+  if (gv4)
+    assign_f32_kernel<true><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
+                                                   rq2, nullptr, fidx, nfull);
+  else
+    assign_f32_kernel<false><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
+                                                    rq2, nullptr, fidx, nfull);
+  if (v4)
+    refine_cands_kernel<true><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq2, labels, mindist, false);
+  else
+    refine_cands_kernel<false><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq2, labels, mindist, false);
+  refine_full_kernel<<<num_sms * 4, 256, 0, s>>>(X, Ct, d, k, st, rq2, labels, mindist, false);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }

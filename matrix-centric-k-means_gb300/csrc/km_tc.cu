@@ -59,7 +59,7 @@ struct TcSmem {
   int abort;
 };
 
-template <bool X3>
+template <int MODE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
                  const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo,
@@ -67,14 +67,16 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
                  uint32_t k, uint32_t kp, uint32_t KB, uint32_t S, uint32_t nalloc, TieBound tb,
                  DevState* st, uint32_t* __restrict__ labels, float* __restrict__ mindist,
                  RefineQueues rq, float* __restrict__ Dout) {
+  constexpr bool ALO = MODE == TC_SPLIT3;      // point operand has a lo part
+  constexpr bool BLO = MODE != TC_PLAIN;       // centroid operand has a lo part
   if (st->done) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
   const uint32_t b_bytes = KB * kp * 128u;              // one of hi / lo
   uint8_t* sB = smem;
-  uint8_t* sA = smem + b_bytes * (X3 ? 2u : 1u);
-  const uint32_t unit_bytes = A_UNIT * (X3 ? 2u : 1u);
+  uint8_t* sA = smem + b_bytes * (BLO ? 2u : 1u);
+  const uint32_t unit_bytes = A_UNIT * (ALO ? 2u : 1u);
   float* cns = reinterpret_cast<float*>(sA + (size_t)S * unit_bytes);
   TcSmem* ts = reinterpret_cast<TcSmem*>(cns + ((kp + 63) & ~63u));
 
@@ -109,11 +111,12 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
     if (lane == 0) {
       tma_prefetch_desc(&tmA);
       tma_prefetch_desc(&tmB);
-      if (X3) { tma_prefetch_desc(&tmAlo); tma_prefetch_desc(&tmBlo); }
-      mbar_arrive_expect_tx(&ts->bfull, b_bytes * (X3 ? 2u : 1u));
+      if (ALO) tma_prefetch_desc(&tmAlo);
+      if (BLO) tma_prefetch_desc(&tmBlo);
+      mbar_arrive_expect_tx(&ts->bfull, b_bytes * (BLO ? 2u : 1u));
       for (uint32_t kb = 0; kb < KB; ++kb) {
         tma_load_2d(sB + (size_t)kb * kp * 128u, &tmB, (int)(kb * 64), 0, &ts->bfull);
-        if (X3) tma_load_2d(sB + b_bytes + (size_t)kb * kp * 128u, &tmBlo, (int)(kb * 64), 0, &ts->bfull);
+        if (BLO) tma_load_2d(sB + b_bytes + (size_t)kb * kp * 128u, &tmBlo, (int)(kb * 64), 0, &ts->bfull);
       }
       uint64_t u = 0;
       bool ok = true;
@@ -124,7 +127,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
           mbar_arrive_expect_tx(&ts->full[s], unit_bytes);
           uint8_t* dst = sA + (size_t)s * unit_bytes;
           tma_load_2d(dst, &tmA, (int)(kb * 64), (int)(tile * TC_M), &ts->full[s]);
-          if (X3) tma_load_2d(dst + A_UNIT, &tmAlo, (int)(kb * 64), (int)(tile * TC_M), &ts->full[s]);
+          if (ALO) tma_load_2d(dst + A_UNIT, &tmAlo, (int)(kb * 64), (int)(tile * TC_M), &ts->full[s]);
         }
       }
       // Drain: every issued copy must land before the CTA exits (these waits
@@ -162,12 +165,8 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
             const uint64_t ad = smem_desc_sw128(a0 + kk * 32u);
             const uint64_t bd = smem_desc_sw128(b0 + kk * 32u);
             tc_mma_bf16(dt, ad, bd, idesc, (kb | kk) != 0u ? 1u : 0u);
-            if (X3) {
-              const uint64_t adl = smem_desc_sw128(a0 + A_UNIT + kk * 32u);
-              const uint64_t bdl = smem_desc_sw128(b0 + b_bytes + kk * 32u);
-              tc_mma_bf16(dt, ad, bdl, idesc, 1u);
-              tc_mma_bf16(dt, adl, bd, idesc, 1u);
-            }
+            if (BLO) tc_mma_bf16(dt, ad, smem_desc_sw128(b0 + b_bytes + kk * 32u), idesc, 1u);
+            if (ALO) tc_mma_bf16(dt, smem_desc_sw128(a0 + A_UNIT + kk * 32u), bd, idesc, 1u);
           }
           tc_commit(&ts->empty[s]);
           issued = true;
@@ -293,19 +292,20 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
 // stays in L2): for each band every CTA takes its T tiles and, for each
 // chunk j, loads chunk j of the centroids (one B slot per 64-column K block,
 // each slot reloaded as soon as the MMAs of the previous chunk have read it)
-// and runs its T tiles against it.  Each row keeps a running state across the
-// chunks in shared memory: the running minimum m and up to four candidates
-// (index, value) with value <= tau(m); when a chunk lowers m the list is
-// filtered with the new tau (tau grows with m, so what survives is exactly
-// {c : v(c) <= tau(m)} over the chunks seen), and more than four candidates
-// marks the row for the full re-score.  After the last chunk the row gets the
-// same treatment as in the single-chunk kernel: one candidate = proven label,
-// 2..4 = exact re-score of those, otherwise full re-score.
+// and runs its T tiles against it.  Each row keeps its running minimum m in
+// shared memory and appends every centroid with v(c) <= tau(m) to its own
+// list of up to L (index, value) pairs in global memory.  tau grows with m and
+// m only falls, so after the last chunk the entries with v(c) <= tau(m_final)
+// are exactly the candidate set of all k centroids; a full list is first
+// compacted with the current tau, and a list that still overflows sends the
+// row to the full re-score.  Final classification: one candidate = proven
+// label, 2..4 = the short re-score queue, 5..L = the wide queue (one warp per
+// row re-scores its list), otherwise the full re-score.
 //
 // Tile i of a band always goes to epilogue set i % 2 and TMEM buffer i % 2,
 // so a row's state is only touched by one thread.
 // ---------------------------------------------------------------------------
-constexpr uint32_t TCC_OVF = 0xffu;     // candidate list overflowed
+constexpr uint32_t TCC_OVF = 0xffffffffu;     // candidate list overflowed
 
 struct TcSmemC {
   uint64_t full[16];
@@ -319,9 +319,9 @@ struct TcSmemC {
   int abort;
 };
 
-__host__ __device__ constexpr uint32_t tcc_state_bytes(uint32_t T) { return T * TC_M * 40u; }
+__host__ __device__ constexpr uint32_t tcc_state_bytes(uint32_t T) { return T * TC_M * 8u; }
 
-template <bool X3>
+template <int MODE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
                          const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo,
@@ -329,6 +329,8 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
                          uint32_t k, uint32_t kp, uint32_t NC, uint32_t KB, uint32_t S, uint32_t T,
                          TieBound tb, DevState* st, uint32_t* __restrict__ labels,
                          float* __restrict__ mindist, RefineQueues rq, float* __restrict__ Dout) {
+  constexpr bool ALO = MODE == TC_SPLIT3;
+  constexpr bool BLO = MODE != TC_PLAIN;
   if (st->done) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -336,14 +338,12 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
   const uint32_t slot_bytes = NC * 128u;                // one 64-column K block of NC centroids
   const uint32_t b_bytes = KB * slot_bytes;             // one of hi / lo
   uint8_t* sB = smem;
-  uint8_t* sA = smem + b_bytes * (X3 ? 2u : 1u);
-  const uint32_t unit_bytes = A_UNIT * (X3 ? 2u : 1u);
+  uint8_t* sA = smem + b_bytes * (BLO ? 2u : 1u);
+  const uint32_t unit_bytes = A_UNIT * (ALO ? 2u : 1u);
   uint8_t* sState = sA + (size_t)S * unit_bytes;
   const uint32_t rows_T = T * TC_M;
-  float* st_m = reinterpret_cast<float*>(sState);
-  uint32_t* st_cnt = reinterpret_cast<uint32_t*>(st_m + rows_T);
-  uint32_t* st_c = st_cnt + rows_T;                     // [4][rows_T]
-  float* st_v = reinterpret_cast<float*>(st_c + 4u * rows_T);
+  float* st_m = reinterpret_cast<float*>(sState);       // running minimum per row
+  uint32_t* st_cnt = reinterpret_cast<uint32_t*>(st_m + rows_T);   // entries in the row's list
   TcSmemC* ts = reinterpret_cast<TcSmemC*>(sState + tcc_state_bytes(T));
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -386,7 +386,8 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
     if (lane == 0) {
       tma_prefetch_desc(&tmA);
       tma_prefetch_desc(&tmB);
-      if (X3) { tma_prefetch_desc(&tmAlo); tma_prefetch_desc(&tmBlo); }
+      if (ALO) tma_prefetch_desc(&tmAlo);
+      if (BLO) tma_prefetch_desc(&tmBlo);
       uint64_t u = 0, p = 0;
       bool ok = true;
       for (uint64_t b = 0; ok; ++b) {
@@ -397,9 +398,9 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
             if (p > 0 && !mbar_wait_bounded(&ts->bempty[kb], (uint32_t)((p - 1) & 1u), abort_flag, WAIT_NS)) {
               fail(11); ok = false; break;
             }
-            mbar_arrive_expect_tx(&ts->bfull[kb], slot_bytes * (X3 ? 2u : 1u));
+            mbar_arrive_expect_tx(&ts->bfull[kb], slot_bytes * (BLO ? 2u : 1u));
             tma_load_2d(sB + (size_t)kb * slot_bytes, &tmB, (int)(kb * 64), (int)(j * NC), &ts->bfull[kb]);
-            if (X3) tma_load_2d(sB + b_bytes + (size_t)kb * slot_bytes, &tmBlo, (int)(kb * 64), (int)(j * NC),
+            if (BLO) tma_load_2d(sB + b_bytes + (size_t)kb * slot_bytes, &tmBlo, (int)(kb * 64), (int)(j * NC),
                                 &ts->bfull[kb]);
           }
           for (uint32_t i = 0; i < Tc && ok; ++i) {
@@ -410,7 +411,7 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
               mbar_arrive_expect_tx(&ts->full[s], unit_bytes);
               uint8_t* dst = sA + (size_t)s * unit_bytes;
               tma_load_2d(dst, &tmA, (int)(kb * 64), (int)(tile * TC_M), &ts->full[s]);
-              if (X3) tma_load_2d(dst + A_UNIT, &tmAlo, (int)(kb * 64), (int)(tile * TC_M), &ts->full[s]);
+              if (ALO) tma_load_2d(dst + A_UNIT, &tmAlo, (int)(kb * 64), (int)(tile * TC_M), &ts->full[s]);
             }
           }
         }
@@ -461,12 +462,8 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
                 const uint64_t ad = smem_desc_sw128(a0 + kk * 32u);
                 const uint64_t bd = smem_desc_sw128(b0 + kk * 32u);
                 tc_mma_bf16(dt, ad, bd, idesc, (kb | kk) != 0u ? 1u : 0u);
-                if (X3) {
-                  const uint64_t adl = smem_desc_sw128(a0 + A_UNIT + kk * 32u);
-                  const uint64_t bdl = smem_desc_sw128(b0 + b_bytes + kk * 32u);
-                  tc_mma_bf16(dt, ad, bdl, idesc, 1u);
-                  tc_mma_bf16(dt, adl, bd, idesc, 1u);
-                }
+                if (BLO) tc_mma_bf16(dt, ad, smem_desc_sw128(b0 + b_bytes + kk * 32u), idesc, 1u);
+                if (ALO) tc_mma_bf16(dt, smem_desc_sw128(a0 + A_UNIT + kk * 32u), bd, idesc, 1u);
               }
               tc_commit(&ts->empty[s]);
               if (i + 1u == Tc) tc_commit(&ts->bempty[kb]);   // B slot kb free once these complete
@@ -502,14 +499,11 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
           const bool valid = row < n;
           const float x2 = valid ? xn2[row] : 0.0f;
           const uint32_t si = i * TC_M + r;
+          // running minimum and candidate count of this row (list in global memory)
           float m = finf;
-          uint32_t cnt = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
-          float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
-          if (j > 0) {
-            m = st_m[si]; cnt = st_cnt[si];
-            c0 = st_c[si]; c1 = st_c[rows_T + si]; c2 = st_c[2 * rows_T + si]; c3 = st_c[3 * rows_T + si];
-            v0 = st_v[si]; v1 = st_v[rows_T + si]; v2 = st_v[2 * rows_T + si]; v3 = st_v[3 * rows_T + si];
-          }
+          uint32_t cnt = 0;
+          if (j > 0) { m = st_m[si]; cnt = st_cnt[si]; }
+          uint2* lst = rq.wl + (valid ? row : 0) * (uint64_t)rq.L;
           const bool okw = mbar_wait_bounded(&ts->tfull[set], use & 1u, abort_flag, WAIT_NS);
           ++use;
           if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(16); ok = false; break; }
@@ -534,26 +528,10 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
           const float mc = fminf(fminf(m0, m1), fminf(m2, m3));
           const float mn = fminf(m, mc);
           const float tau = tie_tau(x2, mn, cmax, tb);
-          // ---- filter the running list with the new tau (keeps ascending order) ----
-          if (cnt != TCC_OVF) {
-            uint32_t nk = 0, e0 = 0, e1 = 0, e2 = 0, e3 = 0;
-            float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f;
-            const uint32_t ci[4] = {c0, c1, c2, c3};
-            const float cv[4] = {v0, v1, v2, v3};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              if ((uint32_t)e < cnt && cv[e] <= tau) {
-                e0 = (nk == 0) ? ci[e] : e0; w0 = (nk == 0) ? cv[e] : w0;
-                e1 = (nk == 1) ? ci[e] : e1; w1 = (nk == 1) ? cv[e] : w1;
-                e2 = (nk == 2) ? ci[e] : e2; w2 = (nk == 2) ? cv[e] : w2;
-                e3 = (nk == 3) ? ci[e] : e3; w3 = (nk == 3) ? cv[e] : w3;
-                ++nk;
-              }
-            }
-            cnt = nk; c0 = e0; c1 = e1; c2 = e2; c3 = e3; v0 = w0; v1 = w1; v2 = w2; v3 = w3;
-          }
-          // ---- pass 2: this chunk's candidates {c < k : v(c) <= tau} ----
-          const bool collect = tau < finf;                 // tau = +inf only while every value is +inf
+          // ---- pass 2: append this chunk's {c < k : v(c) <= tau} to the row's list ----
+          // Entries of earlier chunks above the final tau are dropped after the
+          // last chunk; tau only falls, so the list is a superset until then.
+          const bool collect = tau < finf && valid;       // tau = +inf only while every value is +inf
           for (uint32_t pr = 0; pr < npair; ++pr) {
             uint32_t acc[64];
             tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
@@ -582,21 +560,25 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
               const uint32_t col0 = j * NC + pr * 64u + (uint32_t)h * 32u;     // global centroid index
               uint32_t mk = collect ? mm[h] : 0u;
               mk &= (col0 >= k) ? 0u : (k - col0 >= 32u ? 0xffffffffu : ((1u << (k - col0)) - 1u));
-              while (mk != 0u) {
+              while (mk != 0u && cnt != TCC_OVF) {
                 const uint32_t bit = (uint32_t)(__ffs(mk) - 1);
                 mk &= mk - 1u;
-                if (cnt == TCC_OVF) break;
-                if (cnt == 4u) { cnt = TCC_OVF; break; }
-                const uint32_t col = col0 + bit;
+                if (cnt == rq.L) {
+                  // full: drop entries of earlier chunks that the current tau excludes
+                  uint32_t kept = 0;
+                  for (uint32_t e = 0; e < cnt; ++e) {
+                    const uint2 en = lst[e];
+                    if (__uint_as_float(en.y) <= tau) { if (kept != e) lst[kept] = en; ++kept; }
+                  }
+                  cnt = kept;
+                  if (cnt == rq.L) { cnt = TCC_OVF; break; }
+                }
                 // the candidate's accumulator by selection (static register indices)
                 uint32_t a = 0u;
 #pragma unroll
                 for (int jj = 0; jj < 32; ++jj) a = ((uint32_t)jj == bit) ? acc[h * 32 + jj] : a;
                 const float vv = fmaf(-2.0f, __uint_as_float(a), __ldg(cnj + pr * 64u + h * 32u + bit));
-                c0 = (cnt == 0) ? col : c0; v0 = (cnt == 0) ? vv : v0;
-                c1 = (cnt == 1) ? col : c1; v1 = (cnt == 1) ? vv : v1;
-                c2 = (cnt == 2) ? col : c2; v2 = (cnt == 2) ? vv : v2;
-                c3 = (cnt == 3) ? col : c3; v3 = (cnt == 3) ? vv : v3;
+                lst[cnt] = make_uint2(col0 + bit, __float_as_uint(vv));
                 ++cnt;
               }
             }
@@ -612,20 +594,35 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
           __syncwarp();
           if (lane == 0) mbar_arrive(&ts->tempty[set]);     // accumulator buffer free
           if (!last) {
-            st_m[si] = mn; st_cnt[si] = cnt;
-            st_c[si] = c0; st_c[rows_T + si] = c1; st_c[2 * rows_T + si] = c2; st_c[3 * rows_T + si] = c3;
-            st_v[si] = v0; st_v[rows_T + si] = v1; st_v[2 * rows_T + si] = v2; st_v[3 * rows_T + si] = v3;
+            st_m[si] = mn;
+            st_cnt[si] = cnt;
           } else {
-            // NaN anywhere leaves cnt == 0; overflow or no candidate: full re-score.
-            const uint32_t cf = (cnt == TCC_OVF) ? 0xffffffffu : cnt;
+            // Final filter with tau(m): keep {c : v(c) <= tau}, compacted in
+            // list order; note the first four for the short queue.
+            uint32_t kept = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+            if (cnt != TCC_OVF) {
+              for (uint32_t e = 0; e < cnt; ++e) {
+                const uint2 en = lst[e];
+                if (__uint_as_float(en.y) <= tau) {
+                  if (kept != e) lst[kept] = en;
+                  c0 = (kept == 0) ? en.x : c0; c1 = (kept == 1) ? en.x : c1;
+                  c2 = (kept == 2) ? en.x : c2; c3 = (kept == 3) ? en.x : c3;
+                  ++kept;
+                }
+              }
+            }
+            // NaN leaves kept == 0: full re-score, as does an overflowed list.
+            const uint32_t cf = (cnt == TCC_OVF) ? TCC_OVF : kept;
             if (valid) {
               labels[row] = c0;
               if (mindist) mindist[row] = mn + x2;
+              if (cf > 4u && cf != 0xffffffffu) rq.wlc[row] = cf;
             }
             RefineEntry e{(uint32_t)row, cf, {c0, c1, c2, c3}};
             const uint64_t seg = row >> 5;
             seg_push(rq.cand, rq.ccnt, seg, valid && cf >= 2u && cf <= 4u, e);
-            seg_push(rq.full, rq.fcnt, seg, valid && (cf == 0u || cf > 4u), (uint32_t)row);
+            seg_push(rq.wide, rq.wcnt, seg, valid && cf > 4u && cf <= rq.L, (uint32_t)row);
+            seg_push(rq.full, rq.fcnt, seg, valid && (cf == 0u || cf > rq.L), (uint32_t)row);
           }
         }
       }
@@ -640,13 +637,12 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
 
 }  // namespace
 
-TcPlan plan_tc(uint32_t dp, uint32_t kp, bool x3, uint64_t n, int num_sms) {
+TcPlan plan_tc(uint32_t dp, uint32_t kp, int mode, uint64_t n, int num_sms) {
   TcPlan p;
   if (dp == 0 || dp % 64 != 0 || kp < 16 || kp > 256 || kp % 16 != 0) return p;
   p.KB = dp / 64;
-  const size_t mult = x3 ? 2 : 1;
-  const size_t b_bytes = (size_t)p.KB * kp * 128 * mult;
-  const size_t unit = (size_t)A_UNIT * mult;
+  const size_t b_bytes = (size_t)p.KB * kp * 128 * (mode != TC_PLAIN ? 2 : 1);
+  const size_t unit = (size_t)A_UNIT * (mode == TC_SPLIT3 ? 2 : 1);
   const size_t fixed = 1024 /*align*/ + ((kp + 63) & ~63u) * 4 + sizeof(TcSmem) + 64;
   const size_t budget = 227 * 1024;
   if (b_bytes + fixed + 2 * unit > budget) return p;
@@ -685,20 +681,20 @@ km_status encode_tmap_bf16(CUtensorMap* tm, const void* base, uint64_t inner, ui
   return r == CUDA_SUCCESS ? KM_OK : KM_ERR_CUDA;
 }
 
-TcPlan plan_tc_chunked(uint32_t dp, uint32_t k, bool x3, uint64_t n, int num_sms) {
+TcPlan plan_tc_chunked(uint32_t dp, uint32_t k, int mode, uint64_t n, int num_sms) {
   TcPlan p;
   if (dp == 0 || dp % 64 != 0 || k == 0) return p;
   const uint32_t KB = dp / 64;
   if (KB > 8) return p;
-  const size_t mult = x3 ? 2 : 1;
-  const size_t unit = (size_t)A_UNIT * mult;
+  const size_t bmult = mode != TC_PLAIN ? 2 : 1, amult = mode == TC_SPLIT3 ? 2 : 1;
+  const size_t unit = (size_t)A_UNIT * amult;
   const size_t budget = 227 * 1024;
   const size_t band_max = 48ull << 20;             // rows of one band stay in L2
   for (uint32_t NC : {256u, 128u}) {
     if (NC == 256u && k <= 128u) continue;         // one 128-wide chunk wastes less
-    const size_t b_bytes = (size_t)KB * NC * 128 * mult;
+    const size_t b_bytes = (size_t)KB * NC * 128 * bmult;
     for (uint32_t T : {8u, 6u, 4u, 2u}) {
-      const size_t band = (size_t)num_sms * T * TC_M * dp * 2 * mult;
+      const size_t band = (size_t)num_sms * T * TC_M * dp * 2 * amult;
       if (band > band_max && T > 2) continue;
       const size_t fixed = 1024 + b_bytes + tcc_state_bytes(T) + sizeof(TcSmemC) + 64;
       if (fixed + 2 * unit > budget) continue;
@@ -722,49 +718,54 @@ TcPlan plan_tc_chunked(uint32_t dp, uint32_t k, bool x3, uint64_t n, int num_sms
   return p;
 }
 
-km_status tc_set_attributes(const TcPlan& pl, bool x3) {
-  if (!pl.ok) return KM_ERR_UNSUPPORTED;
-  if (pl.chunked) {
-    if (x3)
-      KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_chunked_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
-    else
-      KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_chunked_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
-    return KM_OK;
-  }
-  if (x3)
-    KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+namespace {
+template <int MODE>
+km_status set_attr_mode(const TcPlan& pl) {
+  if (pl.chunked)
+    KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_chunked_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
   else
-    KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+    KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
   return KM_OK;
 }
 
-km_status launch_assign_tc(const TcPlan& pl, bool x3, const CUtensorMap& tmA,
+template <int MODE>
+void launch_mode(const TcPlan& pl, const CUtensorMap& tmA, const CUtensorMap& tmAlo, const CUtensorMap& tmB,
+                 const CUtensorMap& tmBlo, const float* cn2, const float* xn2, uint64_t n, uint32_t k,
+                 uint32_t kp, TieBound tb, DevState* st, uint32_t* labels, float* mindist,
+                 const RefineQueues& rq, float* Dout, cudaStream_t s) {
+  if (pl.chunked)
+    assign_tc_chunked_kernel<MODE><<<pl.grid, TC_THREADS, pl.smem, s>>>(
+        tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.NC, pl.KB, pl.stages, pl.T, tb, st, labels,
+        mindist, rq, Dout);
+  else
+    assign_tc_kernel<MODE><<<pl.grid, TC_THREADS, pl.smem, s>>>(
+        tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.KB, pl.stages, pl.nalloc, tb, st, labels,
+        mindist, rq, Dout);
+}
+}  // namespace
+
+km_status tc_set_attributes(const TcPlan& pl, int mode) {
+  if (!pl.ok) return KM_ERR_UNSUPPORTED;
+  switch (mode) {
+    case TC_PLAIN: return set_attr_mode<TC_PLAIN>(pl);
+    case TC_SPLIT3: return set_attr_mode<TC_SPLIT3>(pl);
+    case TC_SPLIT2: return set_attr_mode<TC_SPLIT2>(pl);
+  }
+  return KM_ERR_ARG;
+}
+
+km_status launch_assign_tc(const TcPlan& pl, int mode, const CUtensorMap& tmA,
                            const CUtensorMap& tmAlo, const CUtensorMap& tmB,
                            const CUtensorMap& tmBlo, const float* cn2, const float* xn2,
                            uint64_t n, uint32_t k, uint32_t kp, TieBound tb, DevState* st,
                            uint32_t* labels, float* mindist, const RefineQueues& rq,
                            float* Dout, cudaStream_t s) {
   if (!pl.ok) return KM_ERR_UNSUPPORTED;
-  if (pl.chunked) {
-    if (x3)
-      assign_tc_chunked_kernel<true><<<pl.grid, TC_THREADS, pl.smem, s>>>(
-          tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.NC, pl.KB, pl.stages, pl.T, tb, st, labels,
-          mindist, rq, Dout);
-    else
-      assign_tc_chunked_kernel<false><<<pl.grid, TC_THREADS, pl.smem, s>>>(
-          tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.NC, pl.KB, pl.stages, pl.T, tb, st, labels,
-          mindist, rq, Dout);
-    KM_CUDA_TRY(cudaGetLastError());
-    return KM_OK;
-  }
-  if (x3) {
-    assign_tc_kernel<true><<<pl.grid, TC_THREADS, pl.smem, s>>>(
-        tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.KB, pl.stages, pl.nalloc, tb, st, labels,
-        mindist, rq, Dout);
-  } else {
-    assign_tc_kernel<false><<<pl.grid, TC_THREADS, pl.smem, s>>>(
-        tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.KB, pl.stages, pl.nalloc, tb, st, labels,
-        mindist, rq, Dout);
+  switch (mode) {
+    case TC_PLAIN: launch_mode<TC_PLAIN>(pl, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, tb, st, labels, mindist, rq, Dout, s); break;
+    case TC_SPLIT3: launch_mode<TC_SPLIT3>(pl, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, tb, st, labels, mindist, rq, Dout, s); break;
+    case TC_SPLIT2: launch_mode<TC_SPLIT2>(pl, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, tb, st, labels, mindist, rq, Dout, s); break;
+    default: return KM_ERR_ARG;
   }
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
