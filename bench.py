@@ -505,6 +505,65 @@ def kkm_arm(args):
     }
 
 
+def batch_arm(args):
+    """512 independent Lloyd problems, n log-uniform in [1024, 65536], d in
+    {2, 8, 16, 32, 64, 128, 256}, k uniform in [2, 128] (k < n), one seeded
+    Gaussian blob per cluster (sigma 1, centers U[-5, 5]^d), FP32, 8 seeded
+    restarts each, all in one persistent launch; against a sequential loop of
+    single-problem fits (the FP32 Lloyd handle, one instance after another)."""
+    import helpers
+    km = helpers.km()
+    rng = np.random.default_rng(4000)
+    P, R = 512, 8
+    shapes, Xs = [], []
+    for p in range(P):
+        n = int(np.exp(rng.uniform(np.log(1024), np.log(65536))))
+        d = int(rng.choice([2, 8, 16, 32, 64, 128, 256]))
+        k = min(int(rng.integers(2, 129)), n - 1)
+        shapes.append((n, d, k))
+        Xs.append(km.synth_blobs(n, d, k, -5.0, 5.0, 1.0, 4000 + p, nthreads=os.cpu_count() or 8))
+    b = km.Batch(shapes, restarts=R, seed=0, tol=1e-4, maxiter=300).set_data(Xs)
+    v, tune_ms = b.tune()
+    b.fit()                                          # warm-up
+    clk = Clocks(0)
+    with clk:
+        best, results, ms = b.fit()
+    b.close()
+    iters = sum(r[1] for pr in results for r in pr)
+    # sequential per-problem loop on a sample of problems (all restarts), scaled
+    sample = list(range(0, P, P // 16))[:16]
+    t0 = time.perf_counter()
+    seq_iters = 0
+    for p in sample:
+        n, d, k = shapes[p]
+        for r in range(R):
+            m = km.Lloyd(n, d, k, tol=1e-4, seed=p * R + r, maxiter=300, precision="fp32").set_data(Xs[p])
+            _, _, res = m.fit(want_centroids=False)
+            seq_iters += res.iterations
+            m.close()
+    seq_s = time.perf_counter() - t0
+    work = [n * k * d for (n, d, k) in shapes]
+    seq_frac = sum(work[p] for p in sample) / sum(work)
+    seq_pps = len(sample) / seq_s
+    value = P / (ms / 1e3)
+    names = ["128x8", "128x16", "128x32", "256x8", "256x16", "256x32"]
+    return {
+        "metric": "problems/s (512 uneven Lloyd problems x 8 restarts, one persistent launch)",
+        "value": value, "unit": "problems/s", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched lloyd: 512 problems, n log-U[1024,65536], d in {2..256}, k U[2,128], "
+                               "8 restarts, blobs sigma 1 centers U[-5,5]", "problems": P, "restarts": R,
+                   "points_total": int(sum(n for n, _, _ in shapes)), "parallelism": "single GPU"},
+        "instance_iterations": int(iters),
+        "autotune": {"chosen": names[v], "ms_on_sample": dict(zip(names, tune_ms))},
+        "sequential_loop": {"value": seq_pps, "unit": "problems/s", "sample_problems": len(sample),
+                            "sample_work_fraction": seq_frac,
+                            "note": "km_lloyd FP32 handle per instance, one after another, same seeds"},
+        "speedup_vs_sequential": value / seq_pps,
+        "clocks": clk.summary(), "gpu_launches": 1,
+    }
+
+
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the stage's
 # dominant kernel, from one ncu capture of this command
 # (profiles/lloyd_iteration_n1M_d128_k256_launches.md; averages over the
@@ -527,9 +586,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "bf16x3", "fp32"])
-    ap.add_argument("--workload", default="lloyd", choices=["lloyd", "bigk", "kkm"],
+    ap.add_argument("--workload", default="lloyd", choices=["lloyd", "bigk", "kkm", "batch"],
                     help="lloyd: the headline n=1M d=128 k=256 workload (default); bigk: n=4M d=256 "
-                         "k=4096 BF16 points; kkm: kernel k-means n=65536 d=512 k=64")
+                         "k=4096 BF16 points; kkm: kernel k-means n=65536 d=512 k=64; batch: 512 "
+                         "uneven problems x 8 restarts in one launch")
     ap.add_argument("--rows", type=int, default=0,
                     help="bigk only: fewer rows than the workload's n (a smaller case for profilers)")
     args = ap.parse_args()
@@ -543,7 +603,7 @@ def main():
         return
     if args.workload != "lloyd":
         if rank == 0:
-            line = bigk_arm(args) if args.workload == "bigk" else kkm_arm(args)
+            line = {"bigk": bigk_arm, "kkm": kkm_arm, "batch": batch_arm}[args.workload](args)
             print(json.dumps(line), flush=True)
         return
     if world > 1:

@@ -268,6 +268,56 @@ km_status km_kkm_configure(km_kkm* h, uint64_t maxiter, float tol, int32_t check
 km_status km_kkm_fit(km_kkm* h, const uint32_t* init_labels, uint32_t* labels_out, km_result* res);
 void km_kkm_destroy(km_kkm* h);
 
+/* ---- Batched Lloyd: many independent problems, several restarts each ---- */
+
+/* One problem: n points of d coordinates, k clusters (k <= n, k <= 256,
+ * d * round_up(k, 32) * 4 bytes <= 160 KiB).  Points of all problems are
+ * packed one after the other (problem order, row-major). */
+typedef struct km_batch_problem {
+  uint64_t n;
+  uint32_t d;
+  uint32_t k;
+} km_batch_problem;
+
+typedef struct km_batch_params {
+  uint32_t problems;
+  uint32_t restarts;   /* instances per problem (the reference's -r repeats, here seeded restarts) */
+  int32_t seed;        /* restart r of problem p draws its sample picks with seed + p*restarts + r */
+  float tol;
+  uint64_t maxiter;
+  int32_t device;
+  void* stream;
+} km_batch_params;
+
+typedef struct km_batch_result {
+  uint64_t converged_iter;  /* as the reference's run(): converged iteration or maxiter */
+  uint64_t iterations;
+  double objective;         /* FP64 sum of the final assignment's distances */
+} km_batch_result;
+
+typedef struct km_batch km_batch;
+
+/* No counterpart in the reference (its -r repeats one problem sequentially,
+ * src/main.cu:95-120): every restart of every problem runs the reference CPU
+ * algorithm (seeded sample picks, kmeans.cpp:49-200) with labels and
+ * centroids identical to a single run, all in one persistent kernel launch. */
+km_status km_batch_create(const km_batch_params* p, const km_batch_problem* problems, km_batch** out);
+/* X: all problems' points, packed, host memory. */
+km_status km_batch_set_data(km_batch* h, const float* X);
+/* Times the kernel's tile variants on a sample of the instances and keeps the
+ * fastest (km_batch_fit does this on first use). variant_out / ms (6 doubles)
+ * may be NULL. */
+km_status km_batch_tune(km_batch* h, int32_t* variant_out, double* ms_per_variant);
+/* results: problems*restarts entries (problem-major).  best_labels: the labels
+ * of each problem's lowest-objective restart, packed (n per problem);
+ * best_centroids: k*d per problem, packed.  Any output may be NULL. */
+km_status km_batch_fit(km_batch* h, km_batch_result* results, uint32_t* best_labels,
+                       float* best_centroids, double* fit_ms);
+/* Labels (n) and centroids (k*d) of one instance of the last fit. */
+km_status km_batch_instance_labels(km_batch* h, uint32_t problem, uint32_t restart,
+                                   uint32_t* labels_out, float* centroids_out);
+void km_batch_destroy(km_batch* h);
+
 /* ---- Synthetic data (deterministic on every platform) ---- */
 
 /* Gaussian-blob points: centers uniform in [lo,hi]^d, one blob per point drawn

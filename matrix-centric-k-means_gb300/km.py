@@ -56,6 +56,19 @@ class KkmParams(C.Structure):
 _LIB = None
 
 # Exported symbols with their ctypes signatures (restype, argtypes).
+class BatchProblem(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("d", C.c_uint32), ("k", C.c_uint32)]
+
+
+class BatchParams(C.Structure):
+    _fields_ = [("problems", C.c_uint32), ("restarts", C.c_uint32), ("seed", C.c_int32), ("tol", C.c_float),
+                ("maxiter", C.c_uint64), ("device", C.c_int32), ("stream", C.c_void_p)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("converged_iter", C.c_uint64), ("iterations", C.c_uint64), ("objective", C.c_double)]
+
+
 SIGNATURES = {
     "km_status_str": (C.c_char_p, [C.c_int]),
     "km_version": (C.c_char_p, []),
@@ -86,6 +99,12 @@ SIGNATURES = {
     "km_kkm_set_data": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "km_kkm_fit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Result)]),
     "km_kkm_destroy": (None, [C.c_void_p]),
+    "km_batch_create": (C.c_int, [C.POINTER(BatchParams), C.POINTER(BatchProblem), C.POINTER(C.c_void_p)]),
+    "km_batch_set_data": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "km_batch_tune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "km_batch_fit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "km_batch_instance_labels": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "km_batch_destroy": (None, [C.c_void_p]),
     "km_synth_blobs": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
                                  C.c_double, C.c_double, C.c_double, C.c_int32, C.c_uint64, C.c_int32,
                                  C.c_void_p, C.c_void_p]),
@@ -290,3 +309,65 @@ def update(X, labels, k):
     check(_lib().km_update(_ptr(X), _ptr(labels), n, d, k, _ptr(Cc), _ptr(cnt), _ptr(perm), _ptr(off),
                            torch.cuda.current_stream().cuda_stream), "km_update")
     return Cc, cnt, perm, off
+
+
+class Batch:
+    """Handle over km_batch_*: many independent Lloyd problems (list of (n, d, k)),
+    `restarts` seeded restarts each, in one persistent launch."""
+
+    def __init__(self, shapes, restarts=8, seed=0, tol=1e-4, maxiter=300, device=0, stream=0):
+        self.shapes = [(int(n), int(d), int(k)) for n, d, k in shapes]
+        self.restarts = restarts
+        arr = (BatchProblem * len(self.shapes))(*[BatchProblem(n, d, k) for n, d, k in self.shapes])
+        self.p = BatchParams(len(self.shapes), restarts, seed, tol, maxiter, device, stream or None)
+        h = C.c_void_p()
+        check(_lib().km_batch_create(C.byref(self.p), arr, C.byref(h)), "km_batch_create")
+        self.h = h
+
+    def set_data(self, Xs):
+        """Xs: list of (n, d) float32 arrays, one per problem."""
+        packed = np.concatenate([np.ascontiguousarray(x, np.float32).ravel() for x in Xs])
+        check(_lib().km_batch_set_data(self.h, packed.ctypes.data), "km_batch_set_data")
+        return self
+
+    def tune(self):
+        v = C.c_int32(-1)
+        ms = (C.c_double * 6)()
+        check(_lib().km_batch_tune(self.h, C.byref(v), ms), "km_batch_tune")
+        return v.value, list(ms)
+
+    def fit(self):
+        P, R = len(self.shapes), self.restarts
+        res = (BatchResult * (P * R))()
+        lab = np.empty(sum(n for n, _, _ in self.shapes), np.uint32)
+        cen = np.empty(sum(k * d for _, d, k in self.shapes), np.float32)
+        ms = C.c_double(0)
+        check(_lib().km_batch_fit(self.h, res, lab.ctypes.data, cen.ctypes.data, C.byref(ms)), "km_batch_fit")
+        out, lo, co = [], 0, 0
+        for (n, d, k) in self.shapes:
+            out.append((lab[lo:lo + n], cen[co:co + k * d].reshape(k, d)))
+            lo += n
+            co += k * d
+        results = [[(res[p * R + r].converged_iter, res[p * R + r].iterations, res[p * R + r].objective)
+                    for r in range(R)] for p in range(P)]
+        return out, results, ms.value
+
+    def instance(self, problem, restart):
+        n, d, k = self.shapes[problem]
+        lab = np.empty(n, np.uint32)
+        cen = np.empty((k, d), np.float32)
+        check(_lib().km_batch_instance_labels(self.h, problem, restart, lab.ctypes.data, cen.ctypes.data),
+              "km_batch_instance_labels")
+        return lab, cen
+
+    def close(self):
+        if self.h:
+            _lib().km_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
