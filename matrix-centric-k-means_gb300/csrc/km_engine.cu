@@ -78,7 +78,7 @@ LloydEngine::~LloydEngine() {
   dfree(Cb); dfree(Clo); dfree(labels); dfree(mindist); dfree(queue); dfree(qfull); dfree(Ct);
   dfree(qcnt); dfree(qfcnt); dfree(qwide); dfree(qwcnt); dfree(wlc); dfree(wl);
   dfree(q2); dfree(q2full); dfree(q2cnt); dfree(q2fcnt); dfree(fidx); dfree(nfull);
-  dfree(seghist); dfree(counts); dfree(cstart); dfree(perm); dfree(red_part); dfree(st);
+  dfree(seghist); dfree(counts); dfree(cstart); dfree(order); dfree(perm); dfree(red_part); dfree(st);
   if (h_st) cudaFreeHost(h_st);
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
@@ -197,6 +197,7 @@ km_status LloydEngine::init(uint64_t n_, uint32_t d_, uint32_t k_, int precision
     KM_TRY(dalloc(&seghist, (size_t)k * nseg));
     KM_TRY(dalloc(&counts, k));
     KM_TRY(dalloc(&cstart, (size_t)k + 1));
+    KM_TRY(dalloc(&order, k));
     KM_TRY(dalloc(&perm, n));
   }
   return KM_OK;
@@ -331,7 +332,7 @@ km_status LloydEngine::enqueue_sort(const uint32_t* lab) {
   const unsigned hb = (nseg + sort_wpb - 1) / sort_wpb;
   seg_hist_kernel<<<hb, sort_wpb * 32, sort_smem, stream>>>(lab, n, k, seg, nseg, seghist, st);
   seg_scan_kernel<<<(k * 32 + 255) / 256, 256, 0, stream>>>(seghist, k, nseg, counts, st);
-  cluster_scan_kernel<<<1, 1024, 0, stream>>>(counts, k, cstart, st);
+  cluster_scan_kernel<<<1, 1024, 0, stream>>>(counts, k, cstart, st, k <= 1024u ? order : nullptr);
   seg_scatter_kernel<<<hb, sort_wpb * 32, sort_smem, stream>>>(lab, n, k, seg, nseg, seghist, cstart,
                                                                perm, st);
   KM_CUDA_TRY(cudaGetLastError());
@@ -340,7 +341,8 @@ km_status LloydEngine::enqueue_sort(const uint32_t* lab) {
 
 km_status LloydEngine::enqueue_update_step(float tol) {
   (void)tol;
-  return launch_update_sums(X, perm, cstart, d, k, C, Cn, dsq, objpart, st, stream);
+  return launch_update_sums(X, perm, cstart, d, k, C, Cn, dsq, objpart, st, stream,
+                            k <= 1024u ? order : nullptr);
 }
 
 km_status LloydEngine::enqueue_iteration(const LoopConsts& lc) {

@@ -35,8 +35,9 @@ __global__ void seg_hist_kernel(const uint32_t* labels, uint64_t n, uint32_t k, 
                                 uint32_t nseg, uint32_t* seghist, DevState* st);
 __global__ void seg_scan_kernel(uint32_t* seghist, uint32_t k, uint32_t nseg, uint32_t* counts,
                                 DevState* st);
+// order (nullable, k <= 1024): clusters by descending count, ties by index.
 __global__ void cluster_scan_kernel(const uint32_t* counts, uint32_t k, uint32_t* cstart,
-                                    DevState* st);
+                                    DevState* st, uint32_t* order);
 __global__ void seg_scatter_kernel(const uint32_t* labels, uint64_t n, uint32_t k, uint32_t seg,
                                    uint32_t nseg, const uint32_t* seghist, const uint32_t* cstart,
                                    uint32_t* perm, DevState* st);
@@ -78,9 +79,10 @@ km_status launch_assign_tc(const TcPlan& pl, int mode, const CUtensorMap& tmA,
                            float* Dout, cudaStream_t s);
 
 km_status update_sums_prepare();
+// order (nullable): the clusters' processing order (largest first).
 km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_t* cstart, uint32_t d,
                              uint32_t k, const float* C, float* Cn, float* dsq, double* objpart,
-                             DevState* st, cudaStream_t s);
+                             DevState* st, cudaStream_t s, const uint32_t* order = nullptr);
 
 // ---- engine ----
 struct LloydEngine {
@@ -130,6 +132,7 @@ struct LloydEngine {
   RefineEntry* q2 = nullptr;
   uint32_t *q2full = nullptr, *q2cnt = nullptr, *q2fcnt = nullptr, *fidx = nullptr, *nfull = nullptr;
   TieBound tb32{};
+  uint32_t* order = nullptr;   // clusters by descending size (centroid sums, k <= 1024)
   uint32_t* qwide = nullptr;   // chunked kernel: rows with 5..32 candidates
   uint32_t* qwcnt = nullptr;
   uint32_t* wlc = nullptr;

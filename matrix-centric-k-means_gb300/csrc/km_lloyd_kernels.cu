@@ -642,9 +642,26 @@ __global__ void seg_scan_kernel(uint32_t* __restrict__ seghist, uint32_t k, uint
 // Single block: exclusive scan of the k counts -> cstart[0..k] (CSR row
 // pointers of V).
 __global__ void cluster_scan_kernel(const uint32_t* __restrict__ counts, uint32_t k,
-                                    uint32_t* __restrict__ cstart, DevState* st) {
+                                    uint32_t* __restrict__ cstart, DevState* st,
+                                    uint32_t* __restrict__ order) {
   if (st->done) return;
   __shared__ uint32_t part[1024];
+  __shared__ uint32_t scnt[1024];
+  if (order && k <= 1024u) {
+    // largest cluster first, so that the longest ordered sums start first
+    for (uint32_t c = threadIdx.x; c < k; c += blockDim.x) scnt[c] = counts[c];
+    __syncthreads();
+    for (uint32_t c = threadIdx.x; c < k; c += blockDim.x) {
+      const uint32_t v = scnt[c];
+      uint32_t rank = 0;
+      for (uint32_t o = 0; o < k; ++o) {
+        const uint32_t w = scnt[o];
+        rank += (w > v || (w == v && o < c)) ? 1u : 0u;
+      }
+      order[rank] = c;
+    }
+    __syncthreads();
+  }
   const uint32_t per = (k + blockDim.x - 1) / blockDim.x;
   const uint32_t b = threadIdx.x * per, e = min(k, b + per);
   uint32_t s = 0;
@@ -852,7 +869,7 @@ update_sums_kernel(const float* __restrict__ X, const uint32_t* __restrict__ per
 // before exiting.  Permutation indices are prefetched P batches ahead in
 // registers consumed in place.
 namespace {
-constexpr int BLK_ROWS = 32, BLK_STAGES = 8, BLK_COLS = 32;
+constexpr int BLK_ROWS = 32, BLK_STAGES = 16, BLK_COLS = 32;
 constexpr uint64_t BLK_WAIT_NS = 2000000000ull;
 constexpr size_t BLK_SMEM = (size_t)BLK_STAGES * BLK_ROWS * BLK_COLS * sizeof(float);
 constexpr int BLK_LPR = BLK_COLS / 4;           // lanes per row (16 bytes each)
@@ -863,13 +880,17 @@ __global__ void __launch_bounds__(32 * (1 + BLK_COLS / 32))
 update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict__ perm,
                         const uint32_t* __restrict__ cstart, uint32_t d, uint32_t k,
                         const float* __restrict__ C, float* __restrict__ Cn,
-                        float* __restrict__ dsq, double* __restrict__ objpart, DevState* st) {
+                        float* __restrict__ dsq, double* __restrict__ objpart, DevState* st,
+                        const uint32_t* __restrict__ order) {
   if (st && st->done) return;
   extern __shared__ __align__(128) float ring[];        // [BLK_STAGES][BLK_ROWS][BLK_COLS]
   __shared__ __align__(8) uint64_t full[BLK_STAGES], empty[BLK_STAGES];
   __shared__ int abort_flag;
   const uint32_t nblk = (d + BLK_COLS - 1) / BLK_COLS;
-  const uint32_t c = blockIdx.x / nblk, j0 = (blockIdx.x % nblk) * BLK_COLS;
+  // with an order, CTAs take the largest clusters first (they are scheduled in
+  // index order), so that the longest ordered sums start first
+  const uint32_t c = order ? order[blockIdx.x / nblk] : blockIdx.x / nblk;
+  const uint32_t j0 = (blockIdx.x % nblk) * BLK_COLS;
   const uint32_t w = min((uint32_t)BLK_COLS, d - j0);   // columns of this block (multiple of 4)
   const uint32_t nc = (w + 31) / 32;                    // consumer warps doing work
   const uint32_t s0 = cstart[c], s1 = cstart[c + 1];
@@ -1006,11 +1027,11 @@ km_status update_sums_prepare() {
 // when the chains already outnumber the GPU many times over.
 km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_t* cstart, uint32_t d,
                              uint32_t k, const float* C, float* Cn, float* dsq, double* objpart,
-                             DevState* st, cudaStream_t s) {
+                             DevState* st, cudaStream_t s, const uint32_t* order) {
   if (d % 4 == 0 && reinterpret_cast<uintptr_t>(X) % 16 == 0) {
     const uint64_t ctas = (uint64_t)k * ((d + BLK_COLS - 1) / BLK_COLS);
     update_sums_bulk_kernel<<<(unsigned)ctas, 32 * (1 + BLK_COLS / 32), BLK_SMEM, s>>>(
-        X, perm, cstart, d, k, C, Cn, dsq, objpart, st);
+        X, perm, cstart, d, k, C, Cn, dsq, objpart, st, order);
     KM_CUDA_TRY(cudaGetLastError());
     return KM_OK;
   }

@@ -106,7 +106,7 @@ extern "C" km_status km_update_noalloc(const float* X_dev, const uint32_t* label
   const unsigned hb = (nseg + wpb - 1) / wpb;
   seg_hist_kernel<<<hb, wpb * 32, smem, s>>>(labels_dev, n, k, seg, nseg, seghist, st);
   seg_scan_kernel<<<(k * 32 + 255) / 256, 256, 0, s>>>(seghist, k, nseg, counts, st);
-  cluster_scan_kernel<<<1, 1024, 0, s>>>(counts, k, cstart, st);
+  cluster_scan_kernel<<<1, 1024, 0, s>>>(counts, k, cstart, st, nullptr);
   seg_scatter_kernel<<<hb, wpb * 32, smem, s>>>(labels_dev, n, k, seg, nseg, seghist, cstart, perm, st);
   KM_CUDA_TRY(cudaGetLastError());
   // Labels >= k are rejected before the sums run (the histogram flags them).
