@@ -465,16 +465,11 @@ def kkm_arm(args):
     for kern, params in (("polynomial", dict(gamma=1.0 / d, coef=1.0, degree=2)), ("gaussian", dict(sigma=0.5))):
         for kb16 in (False, True):
             prec = "bf16" if kb16 else "bf16x3"
-            # K build alone (tensor cores, kernel function fused in the epilogue)
-            kb_ms = []
-            for _ in range(2):
-                ms, K = _event_ms(lambda: km.kernel_matrix(Xd, kernel=kern, precision=prec, out_bf16=kb16,
-                                                           **params), stream)
-                kb_ms.append(ms)
-                del K
-            torch.cuda.empty_cache()
             m = km.KernelKMeans(n, d, k, kernel=kern, maxiter=args.steps, precision=prec, k_bf16=kb16,
                                 **params).set_data(Xd)
+            kb_ms = [m.build_ms()]
+            m.set_data(Xd)                                 # second build: warm
+            kb_ms.append(m.build_ms())
             m.fit()                                        # warm-up
             clk = Clocks(0)
             with clk:

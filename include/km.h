@@ -262,6 +262,8 @@ typedef struct km_kkm_params {
 km_status km_kkm_create(const km_kkm_params* p, km_kkm** out);
 /* Builds K from n*d points (host or device). */
 km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device);
+/* Device time of the kernel-matrix build done by the last km_kkm_set_data. */
+km_status km_kkm_build_ms(km_kkm* h, double* ms);
 /* Changes maxiter, tol and the -c stop rule before the next fit. */
 km_status km_kkm_configure(km_kkm* h, uint64_t maxiter, float tol, int32_t check_converged);
 /* init_labels: n host labels, or NULL for the reference's i % k. */

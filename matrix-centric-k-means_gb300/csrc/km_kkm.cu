@@ -338,21 +338,22 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
 // 16-byte (FP32) or 8-byte (BF16) loads.
 // ---------------------------------------------------------------------------
 template <bool KBF16>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 kkm_vk_kernel(const void* __restrict__ K, uint64_t n, uint32_t k, const uint32_t* __restrict__ labels,
               float* __restrict__ E, DevState* st) {
   if (st->done) return;
   extern __shared__ __align__(16) uint8_t kk_smem[];
   uint8_t* lab = kk_smem;                                            // n bytes
-  float* bins = reinterpret_cast<float*>(kk_smem + ((n + 15) & ~15ull));  // [8 warps][k][32]
+  float* bins = reinterpret_cast<float*>(kk_smem + ((n + 15) & ~15ull));  // [warps][k][32]
   for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) lab[i] = (uint8_t)labels[i];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float* B = bins + (size_t)warp * k * 32;
   for (uint32_t c = 0; c < k; ++c) B[c * 32 + lane] = 0.0f;
   __syncwarp();
-  const uint64_t nw = (uint64_t)gridDim.x * 8;
-  for (uint64_t row = (uint64_t)blockIdx.x * 8 + warp; row < n; row += nw) {
+  const uint32_t wpb = blockDim.x >> 5;
+  const uint64_t nw = (uint64_t)gridDim.x * wpb;
+  for (uint64_t row = (uint64_t)blockIdx.x * wpb + warp; row < n; row += nw) {
     // With n % 4 == 0 every row starts 16-byte (FP32) / 8-byte (BF16)
     // aligned: lane l takes columns 4l..4l+3 of each 128-column stride.
     // Otherwise one column per lane with plain loads.
@@ -360,15 +361,27 @@ kkm_vk_kernel(const void* __restrict__ K, uint64_t n, uint32_t k, const uint32_t
     if (KBF16) {
       const __nv_bfloat16* Kr = reinterpret_cast<const __nv_bfloat16*>(K) + row * n;
       if (v4) {
-        for (uint64_t j = (uint64_t)lane * 4; j < n; j += 128) {
-          const uint2 raw = __ldg(reinterpret_cast<const uint2*>(Kr + j));
-          const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw.x));
-          const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw.y));
-          const uint32_t l4 = *reinterpret_cast<const uint32_t*>(lab + j);
-          B[((l4 >> 0) & 255u) * 32 + lane] += a.x;
-          B[((l4 >> 8) & 255u) * 32 + lane] += a.y;
-          B[((l4 >> 16) & 255u) * 32 + lane] += b.x;
-          B[((l4 >> 24) & 255u) * 32 + lane] += b.y;
+        // U loads in flight per lane before the (ordered) bin updates
+        constexpr int U = 16;
+        for (uint64_t j0 = (uint64_t)lane * 4; j0 < n; j0 += 128 * U) {
+          uint2 raw[U];
+          uint32_t l4[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const uint64_t j = j0 + 128ull * u;
+            raw[u] = j < n ? __ldg(reinterpret_cast<const uint2*>(Kr + j)) : make_uint2(0u, 0u);
+            l4[u] = j < n ? *reinterpret_cast<const uint32_t*>(lab + j) : 0u;
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            if (j0 + 128ull * u >= n) break;
+            const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw[u].x));
+            const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw[u].y));
+            B[((l4[u] >> 0) & 255u) * 32 + lane] += a.x;
+            B[((l4[u] >> 8) & 255u) * 32 + lane] += a.y;
+            B[((l4[u] >> 16) & 255u) * 32 + lane] += b.x;
+            B[((l4[u] >> 24) & 255u) * 32 + lane] += b.y;
+          }
         }
       } else {
         for (uint64_t j = lane; j < n; j += 32) B[lab[j] * 32 + lane] += __bfloat162float(Kr[j]);
@@ -376,13 +389,25 @@ kkm_vk_kernel(const void* __restrict__ K, uint64_t n, uint32_t k, const uint32_t
     } else {
       const float* Kr = reinterpret_cast<const float*>(K) + row * n;
       if (v4) {
-        for (uint64_t j = (uint64_t)lane * 4; j < n; j += 128) {
-          const float4 v = __ldg(reinterpret_cast<const float4*>(Kr + j));
-          const uint32_t l4 = *reinterpret_cast<const uint32_t*>(lab + j);
-          B[((l4 >> 0) & 255u) * 32 + lane] += v.x;
-          B[((l4 >> 8) & 255u) * 32 + lane] += v.y;
-          B[((l4 >> 16) & 255u) * 32 + lane] += v.z;
-          B[((l4 >> 24) & 255u) * 32 + lane] += v.w;
+        // U loads in flight per lane before the (ordered) bin updates
+        constexpr int U = 8;
+        for (uint64_t j0 = (uint64_t)lane * 4; j0 < n; j0 += 128 * U) {
+          float4 v[U];
+          uint32_t l4[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const uint64_t j = j0 + 128ull * u;
+            v[u] = j < n ? __ldg(reinterpret_cast<const float4*>(Kr + j)) : make_float4(0.f, 0.f, 0.f, 0.f);
+            l4[u] = j < n ? *reinterpret_cast<const uint32_t*>(lab + j) : 0u;
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            if (j0 + 128ull * u >= n) break;
+            B[((l4[u] >> 0) & 255u) * 32 + lane] += v[u].x;
+            B[((l4[u] >> 8) & 255u) * 32 + lane] += v[u].y;
+            B[((l4[u] >> 16) & 255u) * 32 + lane] += v[u].z;
+            B[((l4[u] >> 24) & 255u) * 32 + lane] += v[u].w;
+          }
         }
       } else {
         for (uint64_t j = lane; j < n; j += 32) B[lab[j] * 32 + lane] += Kr[j];
@@ -505,9 +530,11 @@ struct km_kkm {
   double* part = nullptr;
   int dist_blocks = 0;
   size_t vk_smem = 0;
+  uint32_t vk_warps = 8;          // warps per V.K block: as many as the bins leave room for (<= 16)
   bool ready = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int32_t* h_done = nullptr;
+  double kbuild_ms = 0.0;   // device time of the last kernel-matrix build
 };
 
 namespace km {
@@ -593,9 +620,9 @@ km_status kkm_enqueue_iteration(km_kkm* h, const LoopConsts& lc) {
   const uint32_t k = h->p.k;
   cudaStream_t s = e.stream;
   if (h->p.k_bf16)
-    kkm_vk_kernel<true><<<e.num_sms, 256, h->vk_smem, s>>>(h->K, n, k, h->lab, h->E, e.st);
+    kkm_vk_kernel<true><<<e.num_sms, h->vk_warps * 32, h->vk_smem, s>>>(h->K, n, k, h->lab, h->E, e.st);
   else
-    kkm_vk_kernel<false><<<e.num_sms, 256, h->vk_smem, s>>>(h->K, n, k, h->lab, h->E, e.st);
+    kkm_vk_kernel<false><<<e.num_sms, h->vk_warps * 32, h->vk_smem, s>>>(h->K, n, k, h->lab, h->E, e.st);
   KM_TRY(e.enqueue_sort(h->lab));
   kkm_ctilde_kernel<<<(k * 32 + 255) / 256, 256, 0, s>>>(h->E, k, e.perm, e.cstart, h->ct, e.st);
   kkm_dist_kernel<<<h->dist_blocks, 256, 2 * k * sizeof(float), s>>>(h->E, n, k, e.counts, h->ct, h->nlab,
@@ -636,12 +663,18 @@ km_status km_kkm_create(const km_kkm_params* p, km_kkm** out) {
   KM_TRY(kfn_valid(p->kernel_fn, p->degree, p->sigma));
   const uint64_t nn = p->n * p->n;
   if (nn / p->n != p->n) return KM_ERR_ARG;
-  const size_t vk_smem = ((p->n + 15) & ~15ull) + (size_t)8 * p->k * 32 * sizeof(float);
-  if (vk_smem > 227 * 1024) return KM_ERR_UNSUPPORTED;
+  // per-warp bins (k x 32 floats) next to the byte labels; more warps keep
+  // more K rows in flight
+  const size_t lab_bytes = (p->n + 15) & ~15ull, bin_bytes = (size_t)p->k * 32 * sizeof(float);
+  if (lab_bytes + 8 * bin_bytes > 227 * 1024) return KM_ERR_UNSUPPORTED;
+  uint32_t vk_warps = 8;
+  while (vk_warps < 16 && lab_bytes + (size_t)(vk_warps + 1) * bin_bytes <= 227 * 1024) ++vk_warps;
+  const size_t vk_smem = lab_bytes + (size_t)vk_warps * bin_bytes;
   km_kkm* h = new (std::nothrow) km_kkm();
   if (!h) return KM_ERR_ALLOC;
   h->p = *p;
   h->vk_smem = vk_smem;
+  h->vk_warps = vk_warps;
   km_status s = h->eng.init(p->n, p->d, p->k, p->precision, p->device, p->stream, true);
   auto fail = [&](km_status st) { km_kkm_destroy(h); return st; };
   if (s != KM_OK) return fail(s);
@@ -671,10 +704,23 @@ km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device) {
   if (!h || !X) return KM_ERR_ARG;
   LloydEngine& e = h->eng;
   KM_TRY(e.set_points(X, on_device != 0, true));
+  KM_CUDA_TRY(cudaEventRecord(h->ev0, e.stream));
   KM_TRY(build_kernel_matrix(e, e.X, h->p.n, h->p.d, make_kfn(h->p), h->p.precision, h->p.k_bf16 != 0,
                              h->K, h->diag));
+  KM_CUDA_TRY(cudaEventRecord(h->ev1, e.stream));
+  KM_CUDA_TRY(cudaEventSynchronize(h->ev1));
+  float ms = 0.f;
+  KM_CUDA_TRY(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  h->kbuild_ms = ms;
   KM_TRY(e.check_device_error());
   h->ready = true;
+  return KM_OK;
+}
+
+km_status km_kkm_build_ms(km_kkm* h, double* ms) {
+  if (!h || !ms) return KM_ERR_ARG;
+  if (!h->ready) return KM_ERR_STATE;
+  *ms = h->kbuild_ms;
   return KM_OK;
 }
 

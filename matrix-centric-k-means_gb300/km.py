@@ -78,6 +78,7 @@ SIGNATURES = {
     "km_lloyd_init": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "km_lloyd_set_data_bf16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "km_kkm_configure": (C.c_int, [C.c_void_p, C.c_uint64, C.c_float, C.c_int32]),
+    "km_kkm_build_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "km_lloyd_create": (C.c_int, [C.POINTER(LloydParams), C.POINTER(C.c_void_p)]),
     "km_lloyd_set_data": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "km_lloyd_fit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Result)]),
@@ -255,6 +256,12 @@ class KernelKMeans:
         else:
             check(_lib().km_kkm_set_data(self.h, X.data_ptr(), 1), "km_kkm_set_data")
         return self
+
+    def build_ms(self):
+        """Device time of the kernel-matrix build of the last set_data."""
+        ms = C.c_double(0)
+        check(_lib().km_kkm_build_ms(self.h, C.byref(ms)), "km_kkm_build_ms")
+        return ms.value
 
     def fit(self, init_labels=None):
         lab = np.empty(self.p.n, np.uint32)
