@@ -10,7 +10,9 @@ convergence and objective reductions.
                     [--precision bf16|bf16x3|fp32]
 
 --impl ours (default) prints one JSON line: `value` = iterations/s of the
-BF16 tensor-core + exact-refinement path with the points resident in HBM
+split-BF16x3 tensor-core + exact-refinement path (hi*hi + hi*lo + lo*hi,
+FP32 accumulate; --precision bf16 for the single-BF16 form) with the points
+resident in HBM
 (device-timed with CUDA events on the launching stream), the FP32 plain path
 beside it, labels compared between the two, `roofline` for the dominant kernel,
 `e2e` through the C ABI from pinned host memory, `cpu_baseline` (the oracle port
@@ -189,8 +191,9 @@ def ours_arm(args, rank, world):
     labels = {}
     timing = {}
     barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
+    others = [q for q in ("bf16", "bf16x3") if q != args.precision]
     with torch.cuda.stream(stream):
-        for prec in (args.precision, "fp32"):
+        for prec in [args.precision, "fp32"] + others:
             m = km.Lloyd(N, D, K, tol=TOL, seed=KM_SEED, maxiter=args.warmup, precision=prec,
                          conv="none", device=dev, stream=stream.cuda_stream).set_data(Xd)
             m.fit(want_centroids=False)                         # warm-up iterations (graph built)
@@ -301,6 +304,10 @@ def ours_arm(args, rank, world):
         "config": bench_config(world),
         "precision": args.precision,
         "fp32_plain": {"value": fp32_ips, "unit": "iters/s", "stages_ms": stages32},
+        "other_tc_forms": {q: {"value": timing[q]["iters"] / (timing[q]["ms_loop"] / 1000.0), "unit": "iters/s",
+                               "label_agreement_vs_fp32": float((labels[q] == labels["fp32"]).mean()),
+                               "refined_rows_per_iter": timing[q]["refined"] / max(1, timing[q]["iters"])}
+                           for q in others},
         "speedup_vs_fp32_plain": value / world / fp32_ips,
         "label_agreement_vs_fp32": agree,
         "refined_rows_per_iter": timing[args.precision]["refined"] / max(1, iters),
@@ -564,13 +571,15 @@ def batch_arm(args):
 # (profiles/lloyd_iteration_n1M_d128_k256_launches.md; averages over the
 # launches of each arm).  Keys: (precision, stage).
 TRAFFIC = {
-    ("bf16", "distance+argmin"): 282.6e6,        # assign_tc_kernel<0>
-    ("bf16", "refine"): 136.5e6 + 6.6e6,         # refine_cands_kernel + refine_full_kernel
-    ("bf16", "label sort"): 10.6e6,              # seg_hist + seg_scan + cluster_scan + seg_scatter
-    ("bf16", "centroid sums"): 541.8e6,          # update_sums_bulk_kernel
-    ("bf16", "finalize+control"): 0.7e6,
-    ("fp32", "distance+argmin"): 549.2e6,        # assign_f32_kernel<1>
-    ("fp32", "centroid sums"): 541.9e6,
+    ("bf16x3", "distance+argmin"): 550.5e6,      # assign_tc_kernel<1>
+    ("bf16x3", "refine"): 74.4e6 + 2.8e6,        # refine_cands_kernel + refine_full_kernel
+    ("bf16x3", "label sort"): 10.6e6,            # seg_hist + seg_scan + cluster_scan + seg_scatter
+    ("bf16x3", "centroid sums"): 541.7e6,        # update_sums_bulk_kernel
+    ("bf16x3", "finalize+control"): 0.7e6,
+    ("bf16", "distance+argmin"): 283.0e6,        # assign_tc_kernel<0>
+    ("bf16", "centroid sums"): 541.7e6,
+    ("fp32", "distance+argmin"): 549.1e6,        # assign_f32_kernel<1>
+    ("fp32", "centroid sums"): 541.6e6,
 }
 
 
@@ -580,7 +589,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="bf16", choices=["bf16", "bf16x3", "fp32"])
+    ap.add_argument("--precision", default="bf16x3", choices=["bf16", "bf16x3", "fp32"])
     ap.add_argument("--workload", default="lloyd", choices=["lloyd", "bigk", "kkm", "batch"],
                     help="lloyd: the headline n=1M d=128 k=256 workload (default); bigk: n=4M d=256 "
                          "k=4096 BF16 points; kkm: kernel k-means n=65536 d=512 k=64; batch: 512 "
