@@ -50,6 +50,26 @@ __device__ __forceinline__ float kfn_apply(const KFn& f, float dot, float ni, fl
   }
 }
 
+// The same functions with the kind fixed at compile time (one small body per
+// kernel-matrix instantiation; the tensor-core epilogue unrolls it per column).
+template <int KIND>
+__device__ __forceinline__ float kfn_apply_k(const KFn& f, float dot, float ni, float nj) {
+  if constexpr (KIND == KM_KERNEL_LINEAR) {
+    return dot;
+  } else if constexpr (KIND == KM_KERNEL_POLY) {
+    const float b = fmaf(f.gamma, dot, f.coef);
+    float r = 1.0f;
+#pragma unroll 1
+    for (int e = 0; e < f.degree; ++e) r *= b;
+    return r;
+  } else if constexpr (KIND == KM_KERNEL_SIGMOID) {
+    return tanhf(fmaf(f.gamma, dot, f.coef));
+  } else {
+    const float d2 = fmaxf(ni + nj - 2.0f * dot, 0.0f);
+    return expf(-d2 * f.inv2s2);
+  }
+}
+
 // ||x_i||^2 of the operands the tensor cores see (hi, or hi + lo): the
 // Gaussian epilogue's ||x_i||^2 + ||x_j||^2 - 2 x_i.x_j is then the squared
 // distance of those operands (K_ii = 1 exactly), instead of mixing FP32 norms
@@ -147,6 +167,17 @@ constexpr uint32_t KA_BYTES = KM_M * 128;   // 64-column BF16 K-block of A
 constexpr uint32_t KB_BYTES = KM_N * 128;   // 64-column BF16 K-block of B
 constexpr uint64_t KWAIT_NS = 2000000000ull;
 
+constexpr uint64_t KM_GROUP = 16;   // row tiles per raster group of the kernel-matrix build
+
+__device__ __forceinline__ void kmat_tile(uint64_t tile, uint64_t mt, uint64_t nt, uint64_t& mi, uint64_t& nj) {
+  const uint64_t g = tile / (KM_GROUP * nt), r = tile % (KM_GROUP * nt);
+  const uint64_t rows = (mt - g * KM_GROUP) < KM_GROUP ? (mt - g * KM_GROUP) : KM_GROUP;   // last group
+  nj = r / rows;
+  mi = g * KM_GROUP + r % rows;
+}
+
+constexpr uint32_t KM_STG_BYTES = 8u * 32u * 32u * 4u;   // epilogue staging tiles, one per epilogue warp
+
 struct KmSmem {
   uint64_t full[8];
   uint64_t empty[8];
@@ -158,7 +189,7 @@ struct KmSmem {
 };
 }  // namespace
 
-template <bool X3, bool OUT_BF16>
+template <bool X3, bool OUT_BF16, int KIND>
 __global__ void __launch_bounds__(384, 1)
 kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tAlo,
                const __grid_constant__ CUtensorMap tB, const __grid_constant__ CUtensorMap tBlo,
@@ -168,7 +199,8 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
   const uint32_t stage_bytes = (KA_BYTES + KB_BYTES) * (X3 ? 2u : 1u);
-  KmSmem* ts = reinterpret_cast<KmSmem*>(smem + (size_t)S * stage_bytes);
+  float* stg_all = reinterpret_cast<float*>(smem + (size_t)S * stage_bytes);    // [8 warps][32][32]
+  KmSmem* ts = reinterpret_cast<KmSmem*>(smem + (size_t)S * stage_bytes + KM_STG_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t mt = (n + KM_M - 1) / KM_M, nt = (n + KM_N - 1) / KM_N;
   const uint64_t ntiles = mt * nt;
@@ -189,13 +221,15 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
     ts->abort = 1;
     if (atomicOr(&st->err, KM_DEVERR_TIMEOUT) == 0u) st->err_where = 100u + where;
   };
-  // tile t -> (mi, nj), row tiles outermost so that B tiles are reused from L2
+  // tile t -> (mi, nj): groups of KM_GROUP row tiles, column tiles in the
+  // inner loop, so that a group's A tiles stay in L2 while X streams once per group
   if (warp == 0) {
     if (lane == 0) {
       uint64_t u = 0;
       bool ok = true;
       for (uint64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const uint64_t mi = tile / nt, nj = tile % nt;
+        uint64_t mi, nj;
+        kmat_tile(tile, mt, nt, mi, nj);
         for (uint32_t kb = 0; kb < KB; ++kb, ++u) {
           const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
           if (!mbar_wait_bounded(&ts->empty[s], ph ^ 1u, abort_flag, KWAIT_NS)) { fail(1); ok = false; break; }
@@ -261,59 +295,76 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
     uint64_t t = (uint64_t)set;
     for (uint64_t tile = blockIdx.x + (uint64_t)set * gridDim.x; tile < ntiles;
          tile += 2ull * gridDim.x, t += 2) {
-      const uint64_t mi = tile / nt, nj = tile % nt;
+      uint64_t mi, nj;
+        kmat_tile(tile, mt, nt, mi, nj);
       const uint64_t row = mi * KM_M + r, c0 = nj * KM_N;
       const float ni = (row < n) ? xn2[row] : 0.0f;
       // column norms only matter for the Gaussian kernel (broadcast loads)
       auto colnorm = [&](uint64_t c) -> float {
-        return (f.kind == KM_KERNEL_GAUSSIAN && c < n) ? __ldg(xn2 + c) : 0.0f;
+        return (KIND == KM_KERNEL_GAUSSIAN && c < n) ? __ldg(xn2 + c) : 0.0f;
       };
       const bool okw = mbar_wait_bounded(&ts->tfull[set], (uint32_t)(t >> 1) & 1u, abort_flag, KWAIT_NS);
       if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(4); break; }
       tc_fence_after();
+      // Values of this lane's row go to the warp's staging tile (32 rows x 32
+      // columns, 16-byte chunks XOR-swizzled by row) and leave as whole
+      // 128-byte row segments: eight lanes per row, four rows per store.
+      float* stg = stg_all + (size_t)(warp - 4) * 32 * 32;
+      const uint64_t row0 = mi * KM_M + (uint64_t)q * 32u;          // first row of this warp
       for (uint32_t pr = 0; pr < KM_N / 64; ++pr) {
         uint32_t acc[64];
         tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
         tmem_ld_wait();
-        if (row < n) {
-          const uint64_t cb = c0 + pr * 64u;
-          if (OUT_BF16) {
-            __nv_bfloat16* Kr = reinterpret_cast<__nv_bfloat16*>(K) + row * n + cb;
 #pragma unroll
-            for (int j = 0; j < 64; j += 2) {
-              const float v0 = kfn_apply(f, __uint_as_float(acc[j]), ni, colnorm(cb + j));
-              const float v1 = kfn_apply(f, __uint_as_float(acc[j + 1]), ni, colnorm(cb + j + 1));
-              if (vec && cb + j + 1 < n) {
-                *reinterpret_cast<__nv_bfloat162*>(Kr + j) = __floats2bfloat162_rn(v0, v1);
-              } else {
-                if (cb + j < n) Kr[j] = __float2bfloat16_rn(v0);
-                if (cb + j + 1 < n) Kr[j + 1] = __float2bfloat16_rn(v1);
-              }
-              if (diag && cb + j == row) diag[row] = v0;
-              if (diag && cb + j + 1 == row) diag[row] = v1;
+        for (int h = 0; h < 2; ++h) {
+          const uint64_t cb = c0 + pr * 64u + (uint32_t)h * 32u;
+          __syncwarp();                                  // the previous half has been read back
+#pragma unroll
+          for (int c = 0; c < 8; ++c) {
+            float4 o;
+            o.x = kfn_apply_k<KIND>(f, __uint_as_float(acc[h * 32 + 4 * c + 0]), ni, colnorm(cb + 4 * c + 0));
+            o.y = kfn_apply_k<KIND>(f, __uint_as_float(acc[h * 32 + 4 * c + 1]), ni, colnorm(cb + 4 * c + 1));
+            o.z = kfn_apply_k<KIND>(f, __uint_as_float(acc[h * 32 + 4 * c + 2]), ni, colnorm(cb + 4 * c + 2));
+            o.w = kfn_apply_k<KIND>(f, __uint_as_float(acc[h * 32 + 4 * c + 3]), ni, colnorm(cb + 4 * c + 3));
+            if (diag && row < n) {
+              if (cb + 4 * c + 0 == row) diag[row] = o.x;
+              if (cb + 4 * c + 1 == row) diag[row] = o.y;
+              if (cb + 4 * c + 2 == row) diag[row] = o.z;
+              if (cb + 4 * c + 3 == row) diag[row] = o.w;
             }
-          } else {
-            float* Kr = reinterpret_cast<float*>(K) + row * n + cb;
+            *reinterpret_cast<float4*>(stg + lane * 32 + ((c ^ (lane & 7)) * 4)) = o;
+          }
+          __syncwarp();
 #pragma unroll
-            for (int j = 0; j < 64; j += 4) {
-              float4 o;
-              o.x = kfn_apply(f, __uint_as_float(acc[j + 0]), ni, colnorm(cb + j + 0));
-              o.y = kfn_apply(f, __uint_as_float(acc[j + 1]), ni, colnorm(cb + j + 1));
-              o.z = kfn_apply(f, __uint_as_float(acc[j + 2]), ni, colnorm(cb + j + 2));
-              o.w = kfn_apply(f, __uint_as_float(acc[j + 3]), ni, colnorm(cb + j + 3));
-              if (vec && cb + j + 3 < n) {
-                *reinterpret_cast<float4*>(Kr + j) = o;
+          for (int step = 0; step < 8; ++step) {
+            const uint32_t rr = (uint32_t)step * 4u + ((uint32_t)lane >> 3);   // row within the warp's 32
+            const uint32_t ch = (uint32_t)lane & 7u;                           // 16-byte chunk of the row
+            const float4 o = *reinterpret_cast<const float4*>(stg + rr * 32 + ((ch ^ (rr & 7u)) * 4u));
+            const uint64_t grow = row0 + rr, gcol = cb + ch * 4u;
+            if (grow >= n) continue;
+            if (OUT_BF16) {
+              __nv_bfloat16* Kp = reinterpret_cast<__nv_bfloat16*>(K) + grow * n + gcol;
+              if (vec && gcol + 3 < n) {
+                const __nv_bfloat162 a = __floats2bfloat162_rn(o.x, o.y), b = __floats2bfloat162_rn(o.z, o.w);
+                uint2 u;
+                u.x = *reinterpret_cast<const uint32_t*>(&a);
+                u.y = *reinterpret_cast<const uint32_t*>(&b);
+                *reinterpret_cast<uint2*>(Kp) = u;
               } else {
-                if (cb + j + 0 < n) Kr[j + 0] = o.x;
-                if (cb + j + 1 < n) Kr[j + 1] = o.y;
-                if (cb + j + 2 < n) Kr[j + 2] = o.z;
-                if (cb + j + 3 < n) Kr[j + 3] = o.w;
+                if (gcol + 0 < n) Kp[0] = __float2bfloat16_rn(o.x);
+                if (gcol + 1 < n) Kp[1] = __float2bfloat16_rn(o.y);
+                if (gcol + 2 < n) Kp[2] = __float2bfloat16_rn(o.z);
+                if (gcol + 3 < n) Kp[3] = __float2bfloat16_rn(o.w);
               }
-              if (diag) {
-                if (cb + j + 0 == row) diag[row] = o.x;
-                if (cb + j + 1 == row) diag[row] = o.y;
-                if (cb + j + 2 == row) diag[row] = o.z;
-                if (cb + j + 3 == row) diag[row] = o.w;
+            } else {
+              float* Kp = reinterpret_cast<float*>(K) + grow * n + gcol;
+              if (vec && gcol + 3 < n) {
+                *reinterpret_cast<float4*>(Kp) = o;
+              } else {
+                if (gcol + 0 < n) Kp[0] = o.x;
+                if (gcol + 1 < n) Kp[1] = o.y;
+                if (gcol + 2 < n) Kp[2] = o.z;
+                if (gcol + 3 < n) Kp[3] = o.w;
               }
             }
           }
@@ -589,7 +640,7 @@ km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32
   }
   const uint32_t KBn = e.dp / 64;
   const size_t stage = (size_t)(KA_BYTES + KB_BYTES) * (x3 ? 2 : 1);
-  const size_t fixed = 1024 + sizeof(KmSmem) + 64;
+  const size_t fixed = 1024 + KM_STG_BYTES + sizeof(KmSmem) + 64;
   size_t S = (227 * 1024 - fixed) / stage;
   if (S > 8) S = 8;
   if (S < 2) return KM_ERR_UNSUPPORTED;
@@ -597,15 +648,25 @@ km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32
   const uint64_t tiles = ((n + KM_M - 1) / KM_M) * ((n + KM_N - 1) / KM_N);
   const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)e.num_sms);
   const int vec = (n % 4 == 0) && (reinterpret_cast<uintptr_t>(K) % 16 == 0);
-#define KM_LAUNCH_KMAT(X3_, BF_)                                                                   \
+#define KM_LAUNCH_KMAT(X3_, BF_, KIND_)                                                            \
   do {                                                                                             \
-    KM_CUDA_TRY(cudaFuncSetAttribute(kmat_tc_kernel<X3_, BF_>,                                     \
+    KM_CUDA_TRY(cudaFuncSetAttribute(kmat_tc_kernel<X3_, BF_, KIND_>,                              \
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));     \
-    kmat_tc_kernel<X3_, BF_><<<grid, 384, smem, s>>>(tA, tAlo, tB, tBlo, e.xn2, n, KBn, (uint32_t)S, \
-                                                     f, K, diag, vec, e.st);                       \
+    kmat_tc_kernel<X3_, BF_, KIND_><<<grid, 384, smem, s>>>(tA, tAlo, tB, tBlo, e.xn2, n, KBn,     \
+                                                            (uint32_t)S, f, K, diag, vec, e.st);   \
   } while (0)
-  if (x3) { if (out_bf16) KM_LAUNCH_KMAT(true, true); else KM_LAUNCH_KMAT(true, false); }
-  else { if (out_bf16) KM_LAUNCH_KMAT(false, true); else KM_LAUNCH_KMAT(false, false); }
+#define KM_LAUNCH_KIND(X3_, BF_)                                                                   \
+  do {                                                                                             \
+    switch (f.kind) {                                                                              \
+      case KM_KERNEL_LINEAR: KM_LAUNCH_KMAT(X3_, BF_, KM_KERNEL_LINEAR); break;                    \
+      case KM_KERNEL_POLY: KM_LAUNCH_KMAT(X3_, BF_, KM_KERNEL_POLY); break;                        \
+      case KM_KERNEL_SIGMOID: KM_LAUNCH_KMAT(X3_, BF_, KM_KERNEL_SIGMOID); break;                  \
+      default: KM_LAUNCH_KMAT(X3_, BF_, KM_KERNEL_GAUSSIAN); break;                                \
+    }                                                                                              \
+  } while (0)
+  if (x3) { if (out_bf16) KM_LAUNCH_KIND(true, true); else KM_LAUNCH_KIND(true, false); }
+  else { if (out_bf16) KM_LAUNCH_KIND(false, true); else KM_LAUNCH_KIND(false, false); }
+#undef KM_LAUNCH_KIND
 #undef KM_LAUNCH_KMAT
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
