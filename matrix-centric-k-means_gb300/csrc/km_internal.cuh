@@ -263,16 +263,33 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait with a suspend-time hint: the thread may sleep up to hint_ns (or
+// until the phase completes) instead of returning at once.
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
 // Waits for the phase with the given parity to complete, at most `limit_ns`
 // nanoseconds.  Returns false on timeout (or when *abort is raised by a peer).
+// hint_ns > 0 lets a waiting warp sleep between checks, leaving issue slots to
+// the other warps of its scheduler.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
-                                                  volatile int* abort, uint64_t limit_ns) {
+                                                  volatile int* abort, uint64_t limit_ns,
+                                                  uint32_t hint_ns = 0) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
   uint32_t spins = 0;
   while (true) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((++spins & 63u) == 0) {
+    if (hint_ns ? mbar_try_wait_hint(bar, parity, hint_ns) : mbar_try_wait(bar, parity)) return true;
+    if (hint_ns || (++spins & 63u) == 0) {
       if (*abort) return false;
       if (globaltimer_ns() - t0 > limit_ns) return false;
     }
@@ -397,6 +414,21 @@ __device__ __forceinline__ void tmem_ld_32x32b_x64(uint32_t taddr, uint32_t (&r)
         "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
       : "r"(taddr)
       : "memory");
+}
+
+// Three-input minimum (one instruction on sm_100 and later); a NaN input is
+// ignored as by fminf.
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
+// v = c - 2 a for two adjacent accumulator columns in one packed FMA; each
+// half is rounded exactly as fmaf(-2, a, c).
+__device__ __forceinline__ float2 dist_pair(uint32_t a0, uint32_t a1, float c0, float c1) {
+  return __ffma2_rn(make_float2(-2.0f, -2.0f), make_float2(__uint_as_float(a0), __uint_as_float(a1)),
+                    make_float2(c0, c1));
 }
 
 __device__ __forceinline__ void tmem_ld_wait() {

@@ -316,14 +316,24 @@ __device__ __forceinline__ float cpu_dist_v4(const float* __restrict__ x, const 
                                              uint32_t d) {
   const float4* x4 = reinterpret_cast<const float4*>(x);
   const float4* c4 = reinterpret_cast<const float4*>(c);
+  const uint32_t d4 = d / 4;
   float s = 0.0f;
-  for (uint32_t q = 0; q < d / 4; ++q) {
-    const float4 a = x4[q], b = c4[q];
+  auto step = [&](const float4 a, const float4 b) {
     float t = __fsub_rn(a.x, b.x); s = __fadd_rn(s, __fmul_rn(t, t));
     t = __fsub_rn(a.y, b.y); s = __fadd_rn(s, __fmul_rn(t, t));
     t = __fsub_rn(a.z, b.z); s = __fadd_rn(s, __fmul_rn(t, t));
     t = __fsub_rn(a.w, b.w); s = __fadd_rn(s, __fmul_rn(t, t));
+  };
+  uint32_t q = 0;
+  // eight 16-byte loads of each row in flight before the ordered chain uses them
+  for (; q + 8 <= d4; q += 8) {
+    float4 a[8], b[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) { a[i] = x4[q + i]; b[i] = c4[q + i]; }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) step(a[i], b[i]);
   }
+  for (; q < d4; ++q) step(x4[q], c4[q]);
   return s;
 }
 
@@ -331,49 +341,81 @@ __device__ __forceinline__ float cpu_dist_v4(const float* __restrict__ x, const 
 // candidate per lane, the reference's CPU distance (float, j ascending);
 // smallest distance wins, lowest index on ties.  The candidate set provably
 // holds the reference argmin over all k (tie_tau / tie_class).
+// One warp per RC_SEGS consecutive queue segments, their entries flattened so
+// that every pass keeps eight rows in flight; the grid covers all segments at
+// once (no loop over segments, so a warp pays one count load and its rows).
+constexpr int RC_SEGS = 4;
+constexpr int RC_WARPS = 8;
+
 template <bool V4>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32 * RC_WARPS)
 refine_cands_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
                     DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
                     float* __restrict__ mindist, bool count) {
   if (st->done) return;
+  __shared__ uint32_t block_rows;
+  if (threadIdx.x == 0) block_rows = 0;
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  uint32_t done_rows = 0;
-  for (uint64_t seg = warp; seg < rq.nseg; seg += nw) {
-    const uint32_t cnt = rq.ccnt[seg];
-    done_rows += cnt;
-    for (uint32_t base = 0; base < cnt; base += 8) {
-      const uint32_t e = base + (uint32_t)(lane >> 2);
-      const uint32_t slot = lane & 3;
-      float bv = f_inf();
-      uint32_t bi = 0xffffffffu;
-      uint32_t row = 0;
-      if (e < cnt) {
-        const RefineEntry en = rq.cand[seg * 32 + e];
-        row = en.row;
-        if (slot < en.cnt) {
-          const uint32_t c = en.c[slot];
-          const float* x = X + (uint64_t)row * d;
-          const float* cc = C + (uint64_t)c * d;
-          const float v = V4 ? cpu_dist_v4(x, cc, d) : cpu_dist(x, cc, d);
-          if (v < bv) { bv = v; bi = c; }
-        }
-      }
+  const uint64_t seg0 = warp * RC_SEGS;
+  // inclusive prefix of the RC_SEGS segment counts, kept in every lane
+  const uint32_t c = (lane < RC_SEGS && seg0 + (uint64_t)lane < rq.nseg) ? rq.ccnt[seg0 + lane] : 0u;
+  uint32_t pre[RC_SEGS];
+  uint32_t run = 0;
 #pragma unroll
-      for (int o = 1; o <= 2; o <<= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-        const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-      }
-      if (e < cnt && slot == 0) {
-        labels[row] = (bi == 0xffffffffu) ? 0u : bi;
-        if (mindist) mindist[row] = bv;
+  for (int q = 0; q < RC_SEGS; ++q) {
+    run += __shfl_sync(0xffffffffu, c, q);
+    pre[q] = run;
+  }
+  const uint32_t total = run;
+  const uint32_t slot = (uint32_t)lane & 3u;
+  for (uint32_t base = 0; base < total; base += 8) {
+    const uint32_t qi = base + (uint32_t)(lane >> 2);
+    float bv = f_inf();
+    uint32_t bi = 0xffffffffu;
+    uint32_t row = 0;
+    if (qi < total) {
+      uint32_t sg = 0, before = 0;
+#pragma unroll
+      for (int q = 0; q < RC_SEGS - 1; ++q)
+        if (qi >= pre[q]) { sg = (uint32_t)q + 1u; before = pre[q]; }
+      const RefineEntry en = rq.cand[(seg0 + sg) * 32 + (qi - before)];
+      row = en.row;
+      if (slot < en.cnt) {
+        const uint32_t cc = en.c[slot];
+        const float* x = X + (uint64_t)row * d;
+        const float* cr = C + (uint64_t)cc * d;
+        const float v = V4 ? cpu_dist_v4(x, cr, d) : cpu_dist(x, cr, d);
+        if (v < bv) { bv = v; bi = cc; }
       }
     }
+#pragma unroll
+    for (int o = 1; o <= 2; o <<= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+    }
+    if (qi < total && slot == 0) {
+      labels[row] = (bi == 0xffffffffu) ? 0u : bi;
+      if (mindist) mindist[row] = bv;
+    }
   }
-  if (count && lane == 0 && done_rows) atomicAdd(&st->refined_total, (unsigned long long)done_rows);
+  if (count && lane == 0 && total) atomicAdd(&block_rows, total);
+  __syncthreads();
+  if (count && threadIdx.x == 0 && block_rows)
+    atomicAdd(&st->refined_total, (unsigned long long)block_rows);
+}
+
+static void launch_refine_cands(bool v4, const float* X, const float* C, uint32_t d, DevState* st,
+                                const RefineQueues& rq, uint32_t* labels, float* mindist, bool count,
+                                cudaStream_t s) {
+  const uint64_t warps = (rq.nseg + RC_SEGS - 1) / RC_SEGS;
+  const unsigned blocks = (unsigned)std::max<uint64_t>(1, (warps + RC_WARPS - 1) / RC_WARPS);
+  if (v4)
+    refine_cands_kernel<true><<<blocks, 32 * RC_WARPS, 0, s>>>(X, C, d, st, rq, labels, mindist, count);
+  else
+    refine_cands_kernel<false><<<blocks, 32 * RC_WARPS, 0, s>>>(X, C, d, st, rq, labels, mindist, count);
 }
 
 // Exact re-score against all k centroids: one warp per group of up to four
@@ -394,8 +436,15 @@ refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, ui
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   uint32_t done_rows = 0;
-  for (uint64_t seg = warp; seg < rq.nseg; seg += nw) {
-   const uint32_t cnt = rq.fcnt[seg];
+  // 32 segment counts per load; only the non-empty segments are visited
+  for (uint64_t g0 = warp * 32; g0 < rq.nseg; g0 += nw * 32) {
+   const uint32_t cl = (g0 + (uint64_t)lane < rq.nseg) ? rq.fcnt[g0 + lane] : 0u;
+   uint32_t nz = __ballot_sync(0xffffffffu, cl != 0u);
+   while (nz) {
+   const int sl = __ffs(nz) - 1;
+   nz &= nz - 1u;
+   const uint64_t seg = g0 + (uint64_t)sl;
+   const uint32_t cnt = __shfl_sync(0xffffffffu, cl, sl);
    done_rows += cnt;
    for (uint32_t e0 = 0; e0 < cnt; e0 += FULL_ROWS) {
     const uint32_t nr = min(cnt - e0, (uint32_t)FULL_ROWS);
@@ -455,6 +504,7 @@ refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, ui
         if (mindist) mindist[row[r]] = v;
       }
     }
+   }
    }
   }
   if (count && lane == 0 && done_rows) {
@@ -532,10 +582,7 @@ refine_wide_kernel(const float* __restrict__ X, const float* __restrict__ C, uin
 km_status launch_refine(bool v4, int num_sms, const float* X, const float* C, const float* Ct,
                         uint32_t d, uint32_t k, DevState* st, const RefineQueues& rq,
                         uint32_t* labels, float* mindist, cudaStream_t s) {
-  if (v4)
-    refine_cands_kernel<true><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist, true);
-  else
-    refine_cands_kernel<false><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist, true);
+  launch_refine_cands(v4, X, C, d, st, rq, labels, mindist, true, s);
   if (rq.wide) {
     if (v4)
       refine_wide_kernel<true><<<num_sms * 8, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
@@ -552,10 +599,7 @@ km_status launch_refine_gemm(bool v4, int num_sms, const float* X, const float* 
                              TieBound tb32, DevState* st, const RefineQueues& rq,
                              const RefineQueues& rq2, uint32_t* fidx, uint32_t* nfull,
                              uint32_t* labels, float* mindist, cudaStream_t s) {
-  if (v4)
-    refine_cands_kernel<true><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist, true);
-  else
-    refine_cands_kernel<false><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq, labels, mindist, true);
+  launch_refine_cands(v4, X, C, d, st, rq, labels, mindist, true, s);
   if (rq.wide) {
     if (v4)
       refine_wide_kernel<true><<<num_sms * 8, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
@@ -578,10 +622,7 @@ km_status launch_refine_gemm(bool v4, int num_sms, const float* X, const float* 
   else
     assign_f32_kernel<false><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
                                                     rq2, nullptr, fidx, nfull);
-  if (v4)
-    refine_cands_kernel<true><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq2, labels, mindist, false);
-  else
-    refine_cands_kernel<false><<<num_sms * 4, 256, 0, s>>>(X, C, d, st, rq2, labels, mindist, false);
+  launch_refine_cands(v4, X, C, d, st, rq2, labels, mindist, false, s);
   refine_full_kernel<<<num_sms * 4, 256, 0, s>>>(X, Ct, d, k, st, rq2, labels, mindist, false);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
@@ -606,9 +647,19 @@ __global__ void seg_hist_kernel(const uint32_t* __restrict__ labels, uint64_t n,
   if (s < nseg) {
     const uint64_t r0 = (uint64_t)s * seg, r1 = min(n, r0 + seg);
     bool bad = false;
-    for (uint64_t r = r0 + lane; r < r1; r += 32) {
-      const uint32_t l = labels[r];
-      if (l < k) atomicAdd(&cnt[l], 1u); else bad = true;
+    for (uint64_t g = r0; g < r1; g += 32u * 32u) {
+      uint32_t lv[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const uint64_t r = g + (uint64_t)q * 32u + (uint64_t)lane;
+        lv[q] = (r < r1) ? labels[r] : 0u;
+      }
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        if (g + (uint64_t)q * 32u + (uint64_t)lane >= r1) break;
+        const uint32_t l = lv[q];
+        if (l < k) atomicAdd(&cnt[l], 1u); else bad = true;
+      }
     }
     if (bad) atomicOr(&st->err, KM_DEVERR_OVERFLOW);
     __syncwarp();
@@ -625,16 +676,27 @@ __global__ void seg_scan_kernel(uint32_t* __restrict__ seghist, uint32_t k, uint
   if (c >= k) return;
   uint32_t* h = seghist + (uint64_t)c * nseg;
   uint32_t carry = 0;
-  for (uint32_t b = 0; b < nseg; b += 32) {
-    const uint32_t i = b + lane;
-    const uint32_t v = (i < nseg) ? h[i] : 0u;
-    uint32_t x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
+  // groups of 32 coalesced chunks: every load of a group is issued before the
+  // scans that use them
+  for (uint32_t g = 0; g < nseg; g += 32u * 32u) {
+    uint32_t v[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const uint32_t i = g + (uint32_t)q * 32u + (uint32_t)lane;
+      v[q] = (i < nseg) ? h[i] : 0u;
     }
-    if (i < nseg) h[i] = carry + x - v;
-    carry += __shfl_sync(0xffffffffu, x, 31);
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const uint32_t i = g + (uint32_t)q * 32u + (uint32_t)lane;
+      uint32_t x = v[q];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (i < nseg) h[i] = carry + x - v[q];
+      carry += __shfl_sync(0xffffffffu, x, 31);
+    }
   }
   if (lane == 0) counts[c] = carry;
 }
@@ -666,14 +728,28 @@ __global__ void cluster_scan_kernel(const uint32_t* __restrict__ counts, uint32_
   const uint32_t b = threadIdx.x * per, e = min(k, b + per);
   uint32_t s = 0;
   for (uint32_t i = b; i < e; ++i) s += counts[i];
-  part[threadIdx.x] = s;
+  // exclusive block scan of s: warp shuffles, then the warp totals
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) part[wid] = x;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t acc = 0;
-    for (uint32_t t = 0; t < blockDim.x; ++t) { uint32_t v = part[t]; part[t] = acc; acc += v; }
+  if (wid == 0) {
+    const uint32_t nw = blockDim.x >> 5;
+    uint32_t t = (uint32_t)lane < nw ? part[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if ((uint32_t)lane < nw) part[lane] = t;       // inclusive warp totals
   }
   __syncthreads();
-  uint32_t acc = part[threadIdx.x];
+  uint32_t acc = x - s + (wid > 0 ? part[wid - 1] : 0u);
   for (uint32_t i = b; i < e; ++i) { cstart[i] = acc; acc += counts[i]; }
   if (e == k && b < e) cstart[k] = acc;
   if (k == 0 && threadIdx.x == 0) cstart[0] = 0;
@@ -694,10 +770,21 @@ __global__ void seg_scatter_kernel(const uint32_t* __restrict__ labels, uint64_t
   for (uint32_t c = lane; c < k; c += 32) pos[c] = cstart[c] + seghist[(uint64_t)c * nseg + s];
   __syncwarp();
   const uint64_t r0 = (uint64_t)s * seg, r1 = min(n, r0 + seg);
-  for (uint64_t rb = r0; rb < r1; rb += 32) {
+  // labels of up to 32 chunks into registers first (one load latency per group)
+  for (uint64_t g = r0; g < r1; g += 32u * 32u) {
+   uint32_t lv[32];
+#pragma unroll
+   for (int q = 0; q < 32; ++q) {
+     const uint64_t r = g + (uint64_t)q * 32u + (uint64_t)lane;
+     lv[q] = (r < r1) ? labels[r] : 0xffffffffu;
+   }
+#pragma unroll
+   for (int q = 0; q < 32; ++q) {
+    const uint64_t rb = g + (uint64_t)q * 32u;
+    if (rb >= r1) break;
     const uint64_t r = rb + lane;
     const bool valid = r < r1;
-    const uint32_t l = valid ? labels[r] : 0xffffffffu;
+    const uint32_t l = lv[q];
     const bool ok = valid && l < k;
     const unsigned m = __match_any_sync(0xffffffffu, ok ? l : 0xffffffffu);
     const uint32_t rank = __popc(m & ((1u << lane) - 1u));
@@ -708,6 +795,7 @@ __global__ void seg_scatter_kernel(const uint32_t* __restrict__ labels, uint64_t
       if (rank == 0) pos[l] = base + __popc(m);
     }
     __syncwarp();
+   }
   }
 }
 
@@ -858,25 +946,31 @@ update_sums_kernel(const float* __restrict__ X, const uint32_t* __restrict__ per
 }
 
 // Pipelined variant (d % 4 == 0, 16-byte aligned X): one CTA per (cluster,
-// 32-column block), so a cluster's d/32 column chains run on as many SMs and a
-// large cluster is not bound to one SM's outstanding-request capacity.  Warp 0
-// produces: 16-byte cp.async per lane, one instruction copying BLK_RPI row
-// segments, into a BLK_STAGES-deep ring; arrival on the stage's mbarrier fires
-// when its copies land (cp.async.mbarrier.arrive.noinc).  Warp 1 consumes,
-// lane = column: a full batch is loaded into registers first, then summed in
-// row order exactly as the reference (kmeans.cpp:133-137).  Every wait is
-// bounded; on timeout the CTA flags KM_DEVERR_TIMEOUT and drains its copies
-// before exiting.  Permutation indices are prefetched P batches ahead in
-// registers consumed in place.
+// 32-column block), so a cluster's d/32 column chains run on as many SMs.
+// Warps 0..BLK_PROD-1 produce: producer p fills batches p, p + BLK_PROD, ...
+// with 16-byte cp.async per lane (one instruction copies BLK_RPI row segments)
+// into a BLK_STAGES-deep ring; arrival on the stage's mbarrier fires when its
+// copies land (cp.async.mbarrier.arrive.noinc).  A single producer warp caps a
+// CTA at about half the row rate of three.  Warp BLK_PROD consumes, lane =
+// column: a full batch is loaded into registers first, then summed in row
+// order exactly as the reference (kmeans.cpp:133-137).  The objective term is
+// summed per batch in FP32 and across batches as an unevaluated FP32 pair
+// (TwoSum), which keeps FP64-level accuracy without a loop-carried FP64 add
+// (a long-latency operation on this GPU).  Every wait is bounded; on timeout
+// the CTA flags KM_DEVERR_TIMEOUT and drains its copies before exiting.
+// Permutation indices are prefetched P batches ahead in registers consumed in
+// place.
 namespace {
-constexpr int BLK_ROWS = 32, BLK_STAGES = 16, BLK_COLS = 32;
+constexpr int BLK_ROWS = 32, BLK_STAGES = 16, BLK_COLS = 32, BLK_PROD = 3;
 constexpr uint64_t BLK_WAIT_NS = 2000000000ull;
+constexpr uint32_t BLK_SUSPEND_NS = 2000;       // try_wait suspend hint
 constexpr size_t BLK_SMEM = (size_t)BLK_STAGES * BLK_ROWS * BLK_COLS * sizeof(float);
 constexpr int BLK_LPR = BLK_COLS / 4;           // lanes per row (16 bytes each)
 constexpr int BLK_RPI = 32 / BLK_LPR;           // rows per copy instruction
+constexpr int BLK_THREADS = 32 * (BLK_PROD + (BLK_COLS + 31) / 32);
 }  // namespace
 
-__global__ void __launch_bounds__(32 * (1 + BLK_COLS / 32))
+__global__ void __launch_bounds__(BLK_THREADS)
 update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict__ perm,
                         const uint32_t* __restrict__ cstart, uint32_t d, uint32_t k,
                         const float* __restrict__ C, float* __restrict__ Cn,
@@ -908,25 +1002,26 @@ update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict_
     if (st) atomicOr(&st->err, KM_DEVERR_TIMEOUT);
   };
 
-  if (warp == 0) {
-    constexpr int P = 8;
+  if (warp < BLK_PROD) {
+    constexpr int P = 4;
+    const uint32_t p0 = (uint32_t)warp;
     uint32_t pq[P];
 #pragma unroll
     for (int i = 0; i < P; ++i) {
-      const uint32_t idx = s0 + (uint32_t)i * BLK_ROWS + (uint32_t)lane;
-      pq[i] = ((uint32_t)i < nb && idx < s1) ? perm[idx] : 0u;
+      const uint32_t b = p0 + (uint32_t)i * BLK_PROD;
+      const uint32_t idx = s0 + b * BLK_ROWS + (uint32_t)lane;
+      pq[i] = (b < nb && idx < s1) ? perm[idx] : 0u;
     }
     // Unrolled by P so that pq[i] is consumed in place, P batches after its
     // load was issued (moving a register whose load is in flight would wait).
-    uint32_t issued = 0;
     bool ok = true;
-    for (uint32_t b0 = 0; b0 < nb && ok; b0 += P) {
+    for (uint32_t lb0 = 0; p0 + lb0 * BLK_PROD < nb && ok; lb0 += P) {
 #pragma unroll
       for (int i = 0; i < P; ++i) {
-        const uint32_t b = b0 + (uint32_t)i;
+        const uint32_t b = p0 + (lb0 + (uint32_t)i) * BLK_PROD;
         if (b >= nb || !ok) break;
         const uint32_t s = b % BLK_STAGES, ph = (b / BLK_STAGES) & 1u;
-        const bool okw = mbar_wait_bounded(&empty[s], ph ^ 1u, ab, BLK_WAIT_NS);
+        const bool okw = mbar_wait_bounded(&empty[s], ph ^ 1u, ab, BLK_WAIT_NS, BLK_SUSPEND_NS);
         if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(); ok = false; break; }
         const uint32_t m = min((uint32_t)BLK_ROWS, s1 - (s0 + b * BLK_ROWS));
         const uint32_t rl = pq[i];
@@ -950,25 +1045,23 @@ update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict_
           cp_async16_zfill(dst + (size_t)ii * BLK_RPI * BLK_COLS, src, okr ? 16u : 0u);
         }
         cp_async_mbar_arrive_noinc(&full[s]);
-        const uint32_t nbb = b + P;
+        const uint32_t nbb = b + (uint32_t)P * BLK_PROD;
         const uint32_t idx = s0 + nbb * BLK_ROWS + (uint32_t)lane;
         pq[i] = (nbb < nb && idx < s1) ? perm[idx] : 0u;
-        issued = b + 1;
       }
     }
     // Drain: this warp's copies must land before the CTA exits.
     asm volatile("cp.async.wait_all;" ::: "memory");
-    (void)issued;
-  } else if ((uint32_t)warp <= nc) {
-    const uint32_t col = (uint32_t)(warp - 1) * 32u + (uint32_t)lane;   // column within the block
+  } else if ((uint32_t)(warp - BLK_PROD) < nc) {
+    const uint32_t col = (uint32_t)(warp - BLK_PROD) * 32u + (uint32_t)lane;   // column within the block
     const bool vj = col < w;
     const uint64_t p = (uint64_t)c * d + j0 + col;
     const float cold = (C && vj) ? C[p] : 0.0f;
     float sum = 0.0f;
-    double e64 = 0.0;
+    float eh = 0.0f, el = 0.0f;          // objective: FP32 pair hi + lo
     for (uint32_t b = 0; b < nb; ++b) {
       const uint32_t s = b % BLK_STAGES, ph = (b / BLK_STAGES) & 1u;
-      const bool ok = mbar_wait_bounded(&full[s], ph, ab, BLK_WAIT_NS);
+      const bool ok = mbar_wait_bounded(&full[s], ph, ab, BLK_WAIT_NS, BLK_SUSPEND_NS);
       if (!__all_sync(0xffffffffu, ok)) { if (lane == 0) fail(); break; }
       const uint32_t m = min((uint32_t)BLK_ROWS, s1 - (s0 + b * BLK_ROWS));
       const float* src = ring + (size_t)s * BLK_ROWS * BLK_COLS + col;
@@ -993,8 +1086,11 @@ update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict_
           e32 = fmaf(t, t, e32);
         }
       }
-      e32 += e32b;
-      e64 += e32;
+      e32 = __fadd_rn(e32, e32b);
+      // TwoSum: eh + e32 = s_ + err exactly; err accumulates into el
+      const float s_ = __fadd_rn(eh, e32), bb = __fsub_rn(s_, eh);
+      el = __fadd_rn(el, __fadd_rn(__fsub_rn(eh, __fsub_rn(s_, bb)), __fsub_rn(e32, bb)));
+      eh = s_;
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);
     }
@@ -1007,7 +1103,7 @@ update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict_
         const float t = __fsub_rn(cn, cold);
         dsq[p] = __fmul_rn(t, t);
       }
-      if (objpart) objpart[p] = e64;
+      if (objpart) objpart[p] = (double)eh + (double)el;
     }
   }
 }
@@ -1030,7 +1126,7 @@ km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_
                              DevState* st, cudaStream_t s, const uint32_t* order) {
   if (d % 4 == 0 && reinterpret_cast<uintptr_t>(X) % 16 == 0) {
     const uint64_t ctas = (uint64_t)k * ((d + BLK_COLS - 1) / BLK_COLS);
-    update_sums_bulk_kernel<<<(unsigned)ctas, 32 * (1 + BLK_COLS / 32), BLK_SMEM, s>>>(
+    update_sums_bulk_kernel<<<(unsigned)ctas, BLK_THREADS, BLK_SMEM, s>>>(
         X, perm, cstart, d, k, C, Cn, dsq, objpart, st, order);
     KM_CUDA_TRY(cudaGetLastError());
     return KM_OK;
@@ -1089,9 +1185,15 @@ __global__ void finalize_kernel(const float* __restrict__ Cn, float* __restrict_
     mv += __shfl_xor_sync(0xffffffffu, mv, o);
     ob += __shfl_xor_sync(0xffffffffu, ob, o);
   }
+  // Reference shift test: float sum over j ascending.  Coalesced loads of 32
+  // terms, each broadcast in order into the same chain on every lane.
+  float s = 0.0f;
+  for (uint32_t j0 = 0; j0 < d; j0 += 32) {
+    const float t = (j0 + (uint32_t)lane < d) ? dsq[base + j0 + lane] : 0.0f;
+    const uint32_t m = min(32u, d - j0);
+    for (uint32_t q = 0; q < m; ++q) s = __fadd_rn(s, __shfl_sync(0xffffffffu, t, (int)q));
+  }
   if (lane == 0) {
-    float s = 0.0f;
-    for (uint32_t j = 0; j < d; ++j) s = __fadd_rn(s, dsq[base + j]);
     if (sqrtf(s) > tol) st->moved = 1u;
     cn2[c] = excl ? f_inf() : (float)nrm;
     shift_c[c] = sqrt(mv);

@@ -206,15 +206,19 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
         tmem_ld_wait();
         const float4* cn4 = reinterpret_cast<const float4*>(cns + pr * 64u);
 #pragma unroll
-        for (int j4 = 0; j4 < 16; ++j4) {
-          const float4 cc = cn4[j4];
-          m0 = fminf(m0, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 0]), cc.x));
-          m1 = fminf(m1, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 1]), cc.y));
-          m2 = fminf(m2, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 2]), cc.z));
-          m3 = fminf(m3, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 3]), cc.w));
+        for (int j4 = 0; j4 < 16; j4 += 2) {
+          const float4 ca = cn4[j4], cb = cn4[j4 + 1];
+          const float2 va = dist_pair(acc[4 * j4 + 0], acc[4 * j4 + 1], ca.x, ca.y);
+          const float2 vb = dist_pair(acc[4 * j4 + 2], acc[4 * j4 + 3], ca.z, ca.w);
+          const float2 vc = dist_pair(acc[4 * j4 + 4], acc[4 * j4 + 5], cb.x, cb.y);
+          const float2 vd = dist_pair(acc[4 * j4 + 6], acc[4 * j4 + 7], cb.z, cb.w);
+          m0 = fmin3(m0, va.x, va.y);
+          m1 = fmin3(m1, vb.x, vb.y);
+          m2 = fmin3(m2, vc.x, vc.y);
+          m3 = fmin3(m3, vd.x, vd.y);
         }
       }
-      const float v1 = fminf(fminf(m0, m1), fminf(m2, m3));
+      const float v1 = fmin3(m0, m1, fminf(m2, m3));
       const float tau = tie_tau(x2, v1, cmax, tb);
       // ---- pass 2: candidates {c < k : v(c) <= tau}, as 32-column bit masks ----
       uint32_t cnt = 0, got = 0, k0 = 0, k1 = 0, k2 = 0, k3 = 0;
@@ -223,24 +227,21 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
         tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
         tmem_ld_wait();
         const float4* cn4 = reinterpret_cast<const float4*>(cns + pr * 64u);
-        uint32_t mlo = 0, mhi = 0;
+        uint32_t mm[2] = {0u, 0u};
 #pragma unroll
-        for (int j4 = 0; j4 < 8; ++j4) {
-          const float4 cc = cn4[j4];
-          if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 0]), cc.x) <= tau) mlo |= 1u << (4 * j4 + 0);
-          if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 1]), cc.y) <= tau) mlo |= 1u << (4 * j4 + 1);
-          if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 2]), cc.z) <= tau) mlo |= 1u << (4 * j4 + 2);
-          if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 3]), cc.w) <= tau) mlo |= 1u << (4 * j4 + 3);
-        }
+        for (int h = 0; h < 2; ++h) {
 #pragma unroll
-        for (int j4 = 0; j4 < 8; ++j4) {
-          const float4 cc = cn4[8 + j4];
-          if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 0]), cc.x) <= tau) mhi |= 1u << (4 * j4 + 0);
-          if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 1]), cc.y) <= tau) mhi |= 1u << (4 * j4 + 1);
-          if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 2]), cc.z) <= tau) mhi |= 1u << (4 * j4 + 2);
-          if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 3]), cc.w) <= tau) mhi |= 1u << (4 * j4 + 3);
+          for (int j4 = 0; j4 < 8; ++j4) {
+            const float4 cc = cn4[8 * h + j4];
+            const int a = 32 * h + 4 * j4;
+            const float2 va = dist_pair(acc[a + 0], acc[a + 1], cc.x, cc.y);
+            const float2 vb = dist_pair(acc[a + 2], acc[a + 3], cc.z, cc.w);
+            mm[h] |= (va.x <= tau ? 1u : 0u) << (4 * j4 + 0);
+            mm[h] |= (va.y <= tau ? 1u : 0u) << (4 * j4 + 1);
+            mm[h] |= (vb.x <= tau ? 1u : 0u) << (4 * j4 + 2);
+            mm[h] |= (vb.y <= tau ? 1u : 0u) << (4 * j4 + 3);
+          }
         }
-        uint32_t mm[2] = {mlo, mhi};
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const uint32_t c0 = pr * 64u + (uint32_t)h * 32u;
@@ -517,15 +518,19 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
             tmem_ld_wait();
             const float4* cn4 = reinterpret_cast<const float4*>(cnj + pr * 64u);
 #pragma unroll
-            for (int j4 = 0; j4 < 16; ++j4) {
-              const float4 cc = __ldg(cn4 + j4);
-              m0 = fminf(m0, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 0]), cc.x));
-              m1 = fminf(m1, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 1]), cc.y));
-              m2 = fminf(m2, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 2]), cc.z));
-              m3 = fminf(m3, fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 3]), cc.w));
+            for (int j4 = 0; j4 < 16; j4 += 2) {
+              const float4 ca = __ldg(cn4 + j4), cb = __ldg(cn4 + j4 + 1);
+              const float2 va = dist_pair(acc[4 * j4 + 0], acc[4 * j4 + 1], ca.x, ca.y);
+              const float2 vb = dist_pair(acc[4 * j4 + 2], acc[4 * j4 + 3], ca.z, ca.w);
+              const float2 vc = dist_pair(acc[4 * j4 + 4], acc[4 * j4 + 5], cb.x, cb.y);
+              const float2 vd = dist_pair(acc[4 * j4 + 6], acc[4 * j4 + 7], cb.z, cb.w);
+              m0 = fmin3(m0, va.x, va.y);
+              m1 = fmin3(m1, vb.x, vb.y);
+              m2 = fmin3(m2, vc.x, vc.y);
+              m3 = fmin3(m3, vd.x, vd.y);
             }
           }
-          const float mc = fminf(fminf(m0, m1), fminf(m2, m3));
+          const float mc = fmin3(m0, m1, fminf(m2, m3));
           const float mn = fminf(m, mc);
           const float tau = tie_tau(x2, mn, cmax, tb);
           // ---- pass 2: append this chunk's {c < k : v(c) <= tau} to the row's list ----
@@ -537,24 +542,21 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
             tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
             tmem_ld_wait();
             const float4* cn4 = reinterpret_cast<const float4*>(cnj + pr * 64u);
-            uint32_t mlo = 0, mhi = 0;
+            uint32_t mm[2] = {0u, 0u};
 #pragma unroll
-            for (int j4 = 0; j4 < 8; ++j4) {
-              const float4 cc = __ldg(cn4 + j4);
-              if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 0]), cc.x) <= tau) mlo |= 1u << (4 * j4 + 0);
-              if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 1]), cc.y) <= tau) mlo |= 1u << (4 * j4 + 1);
-              if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 2]), cc.z) <= tau) mlo |= 1u << (4 * j4 + 2);
-              if (fmaf(-2.0f, __uint_as_float(acc[4 * j4 + 3]), cc.w) <= tau) mlo |= 1u << (4 * j4 + 3);
-            }
+            for (int h = 0; h < 2; ++h) {
 #pragma unroll
-            for (int j4 = 0; j4 < 8; ++j4) {
-              const float4 cc = __ldg(cn4 + 8 + j4);
-              if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 0]), cc.x) <= tau) mhi |= 1u << (4 * j4 + 0);
-              if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 1]), cc.y) <= tau) mhi |= 1u << (4 * j4 + 1);
-              if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 2]), cc.z) <= tau) mhi |= 1u << (4 * j4 + 2);
-              if (fmaf(-2.0f, __uint_as_float(acc[32 + 4 * j4 + 3]), cc.w) <= tau) mhi |= 1u << (4 * j4 + 3);
+              for (int j4 = 0; j4 < 8; ++j4) {
+                const float4 cc = __ldg(cn4 + 8 * h + j4);
+                const int a = 32 * h + 4 * j4;
+                const float2 va = dist_pair(acc[a + 0], acc[a + 1], cc.x, cc.y);
+                const float2 vb = dist_pair(acc[a + 2], acc[a + 3], cc.z, cc.w);
+                mm[h] |= (va.x <= tau ? 1u : 0u) << (4 * j4 + 0);
+                mm[h] |= (va.y <= tau ? 1u : 0u) << (4 * j4 + 1);
+                mm[h] |= (vb.x <= tau ? 1u : 0u) << (4 * j4 + 2);
+                mm[h] |= (vb.y <= tau ? 1u : 0u) << (4 * j4 + 3);
+              }
             }
-            const uint32_t mm[2] = {mlo, mhi};
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
               const uint32_t col0 = j * NC + pr * 64u + (uint32_t)h * 32u;     // global centroid index
