@@ -134,7 +134,7 @@ km_status LloydEngine::init(uint64_t n_, uint32_t d_, uint32_t k_, int precision
     }
   }
   KM_TRY(dalloc(&C, (size_t)k * d));
-  KM_TRY(dalloc(&cn2, kp));
+  KM_TRY(dalloc(&cn2, (kp + 63) & ~63u));        // padded: +inf up to a multiple of 64
   KM_TRY(dalloc(&labels, n));
   KM_TRY(dalloc(&mindist, n));
   {
@@ -291,8 +291,9 @@ km_status LloydEngine::set_centroids_dev(const float* Csrc) {
   if (Csrc != C)
     KM_CUDA_TRY(cudaMemcpyAsync(C, Csrc, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
   KM_CUDA_TRY(cudaMemsetAsync(&st->cmax, 0, sizeof(float), stream));
-  const int blocks = (int)((kp * 32 + 255) / 256);
-  prep_centroids_kernel<<<blocks, 256, 0, stream>>>(C, k, kp, d, dp, cn2, Cb, Clo, Ct, st);
+  const uint32_t kp64 = (kp + 63) & ~63u;
+  const int blocks = (int)((kp64 * 32 + 255) / 256);
+  prep_centroids_kernel<<<blocks, 256, 0, stream>>>(C, k, kp, d, dp, cn2, Cb, Clo, Ct, st, kp64);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }

@@ -15,7 +15,7 @@ __global__ void reduce_f64_partial_kernel(const double* v, uint64_t n, double* p
 __global__ void reduce_f64_final_kernel(const double* part, int np, double* out);
 __global__ void prep_centroids_kernel(const float* C, uint32_t k, uint32_t kp, uint32_t d,
                                       uint32_t dp, float* cn2, __nv_bfloat16* Cb,
-                                      __nv_bfloat16* Clo, float* Ct, DevState* st);
+                                      __nv_bfloat16* Clo, float* Ct, DevState* st, uint32_t kp64);
 km_status launch_assign_f32(const float* X, const float* C, const float* cn2, const float* xn2,
                             uint64_t n, uint32_t d, uint32_t k, TieBound tb, DevState* st,
                             uint32_t* labels, float* mindist, const RefineQueues& rq,

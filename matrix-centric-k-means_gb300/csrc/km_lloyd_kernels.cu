@@ -91,10 +91,14 @@ __global__ void prep_centroids_kernel(const float* __restrict__ C, uint32_t k, u
                                       uint32_t d, uint32_t dp, float* __restrict__ cn2,
                                       __nv_bfloat16* __restrict__ Cb,
                                       __nv_bfloat16* __restrict__ Clo, float* __restrict__ Ct,
-                                      DevState* st) {
+                                      DevState* st, uint32_t kp64) {
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (warp >= kp) return;
+  if (warp >= kp) {
+    // +inf norms up to whole 64-column groups (read by the distance epilogue)
+    if (warp < kp64 && lane == 0) cn2[warp] = f_inf();
+    return;
+  }
   const uint32_t c = warp;
   double s = 0.0;
   for (uint32_t j = lane; j < dp; j += 32) {
@@ -344,7 +348,7 @@ __device__ __forceinline__ float cpu_dist_v4(const float* __restrict__ x, const 
 // One warp per RC_SEGS consecutive queue segments, their entries flattened so
 // that every pass keeps eight rows in flight; the grid covers all segments at
 // once (no loop over segments, so a warp pays one count load and its rows).
-constexpr int RC_SEGS = 4;
+constexpr int RC_SEGS = 2;
 constexpr int RC_WARPS = 8;
 
 template <bool V4>

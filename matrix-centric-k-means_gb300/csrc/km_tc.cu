@@ -11,14 +11,16 @@
 //   warp 0       TMA producer (one elected lane)
 //   warp 1       MMA issuer (one elected lane)
 //   warp 2       TMEM allocator
-//   warps 4-11   epilogue, two sets of four warps: set s takes the tiles
-//                t = s (mod 2), i.e. TMEM accumulator buffer s, so two tiles
-//                are in the epilogue at once; warp w reads TMEM lanes
-//                32*(w%4)..+31 (its rows) across all kp columns, with no
-//                exchange between warps:
-//                pass 1  row minimum v1 of v = ||c||^2 - 2 acc;
+//   warps 4-11   epilogue, all eight on the same tile: warp w reads TMEM
+//                lanes 32*(w%4)..+31 (its rows) and one half of the kp
+//                columns, so the accumulator buffer is released after half a
+//                row's column work and the MMAs of the next tile on that
+//                buffer start early:
+//                pass 1  partial row minimum of v = ||c||^2 - 2 acc, exchanged
+//                        with the other half: v1;
 //                pass 2  candidates {c : v(c) <= tau(v1)} (tie_tau) as
-//                        per-chunk bit masks (TMEM is read a second time);
+//                        per-chunk bit masks (TMEM is read a second time); the
+//                        upper half hands its count and first candidates over;
 //                one candidate: the label is proven; 2..4: queued for the
 //                exact re-score of those; more: full re-score.
 //
@@ -55,6 +57,7 @@ struct TcSmem {
   uint64_t tfull[2];
   uint64_t tempty[2];
   uint64_t tdone;
+  uint64_t pairbar[4];      // epilogue: the two warps of TMEM lane quadrant q
   uint32_t tmem_base;
   int abort;
 };
@@ -77,8 +80,8 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   uint8_t* sB = smem;
   uint8_t* sA = smem + b_bytes * (BLO ? 2u : 1u);
   const uint32_t unit_bytes = A_UNIT * (ALO ? 2u : 1u);
-  float* cns = reinterpret_cast<float*>(sA + (size_t)S * unit_bytes);
-  TcSmem* ts = reinterpret_cast<TcSmem*>(cns + ((kp + 63) & ~63u));
+  float* xch = reinterpret_cast<float*>(sA + (size_t)S * unit_bytes);   // [2][TC_M] row exchange
+  TcSmem* ts = reinterpret_cast<TcSmem*>(xch + 2 * TC_M);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t ntiles = (n + TC_M - 1) / TC_M;
@@ -87,14 +90,12 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   if (threadIdx.x == 0) {
     for (uint32_t s = 0; s < S; ++s) { mbar_init(&ts->full[s], 1); mbar_init(&ts->empty[s], 1); }
     mbar_init(&ts->bfull, 1);
-    for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], 4); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], TC_EPI_WARPS); }
     mbar_init(&ts->tdone, 1);
+    for (int qq = 0; qq < 4; ++qq) mbar_init(&ts->pairbar[qq], 2);
     ts->abort = 0;
     mbar_fence_init();
   }
-  const uint32_t kp64 = (kp + 63) & ~63u;    // +inf padding up to whole 64-column loads
-  for (uint32_t c = threadIdx.x; c < kp64; c += blockDim.x)
-    cns[c] = (c < k) ? cn2[c] : __int_as_float(0x7f800000);
   if (warp == 2) tmem_alloc(&ts->tmem_base, 2u * nalloc);
   tc_fence_before();
   __syncthreads();
@@ -182,32 +183,45 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       }
     }
   } else if (warp >= 4) {
-    // Epilogue set `set` (0/1) takes the tiles with t % 2 == set, i.e. TMEM
-    // accumulator buffer `set`; warp q = warp % 4 owns TMEM lanes (rows)
-    // 32q..32q+31 and all kp columns of them, so no cross-warp exchange.
-    const int q = warp & 3, set = (warp - 4) >> 2;
-    const uint32_t npair = (kp + 63) / 64;          // <= 4 loads of 64 columns
+    // Epilogue: the eight warps take every tile of this CTA together.  Warp w
+    // owns TMEM lanes (rows) 32*(w%4)..+31 and half h = (w-4)/4 of the 64-column
+    // loads (h = 0 the lower columns), so a tile's accumulator is released after
+    // half the column work of one warp.  The two warps of a quadrant exchange the
+    // row's partial minimum, then the upper half's candidate summary, through
+    // xch and their pair mbarrier (two phases per tile, bounded waits).
+    const int q = warp & 3, h = (warp - 4) >> 2;
+    const uint32_t npair = (kp + 63) / 64;          // 64-column loads in all
+    const uint32_t nlo = (npair + 1) / 2;           // of which half 0 takes the first nlo
+    const uint32_t pr0 = h ? nlo : 0u, pr1 = h ? npair : nlo;
     const uint32_t r = (uint32_t)q * 32u + (uint32_t)lane;
-    const uint32_t tbase = tmem_base + (((uint32_t)q * 32u) << 16) + (uint32_t)set * nalloc;
-    uint64_t t = (uint64_t)set;
-    for (uint64_t tile = blockIdx.x + (uint64_t)set * gridDim.x; tile < ntiles;
-         tile += 2ull * gridDim.x, t += 2) {
-      const uint32_t use = (uint32_t)(t >> 1);
+    uint64_t* pb = &ts->pairbar[q];
+    uint32_t pbuse = 0;                             // completed phases of pb
+    auto pair_sync = [&]() -> bool {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(pb);
+      const bool ok = mbar_wait_bounded(pb, pbuse & 1u, abort_flag, WAIT_NS);
+      ++pbuse;
+      return __all_sync(0xffffffffu, ok);
+    };
+    uint64_t t = 0;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
+      const uint32_t buf = (uint32_t)(t & 1u), use = (uint32_t)(t >> 1);
       const uint64_t row = tile * TC_M + r;
       const float x2 = (row < n) ? xn2[row] : 0.0f;
-      const bool okw = mbar_wait_bounded(&ts->tfull[set], use & 1u, abort_flag, WAIT_NS);
+      const bool okw = mbar_wait_bounded(&ts->tfull[buf], use & 1u, abort_flag, WAIT_NS);
       if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(5); break; }
       tc_fence_after();
-      // ---- pass 1: row minimum of v = ||c||^2 - 2 acc (64 columns per load) ----
+      const uint32_t tbase = tmem_base + (((uint32_t)q * 32u) << 16) + buf * nalloc;
+      // ---- pass 1: partial row minimum of v = ||c||^2 - 2 acc over this half ----
       float m0 = __int_as_float(0x7f800000), m1 = m0, m2 = m0, m3 = m0;
-      for (uint32_t pr = 0; pr < npair; ++pr) {
+      for (uint32_t pr = pr0; pr < pr1; ++pr) {
         uint32_t acc[64];
         tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
         tmem_ld_wait();
-        const float4* cn4 = reinterpret_cast<const float4*>(cns + pr * 64u);
+        const float4* cn4 = reinterpret_cast<const float4*>(cn2 + pr * 64u);
 #pragma unroll
         for (int j4 = 0; j4 < 16; j4 += 2) {
-          const float4 ca = cn4[j4], cb = cn4[j4 + 1];
+          const float4 ca = __ldg(cn4 + j4), cb = __ldg(cn4 + j4 + 1);
           const float2 va = dist_pair(acc[4 * j4 + 0], acc[4 * j4 + 1], ca.x, ca.y);
           const float2 vb = dist_pair(acc[4 * j4 + 2], acc[4 * j4 + 3], ca.z, ca.w);
           const float2 vc = dist_pair(acc[4 * j4 + 4], acc[4 * j4 + 5], cb.x, cb.y);
@@ -218,34 +232,37 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
           m3 = fmin3(m3, vd.x, vd.y);
         }
       }
-      const float v1 = fmin3(m0, m1, fminf(m2, m3));
+      const float mh = fmin3(m0, m1, fminf(m2, m3));
+      xch[h * TC_M + r] = mh;
+      if (!pair_sync()) { if (lane == 0) fail(6); break; }
+      const float v1 = fminf(mh, xch[(1 - h) * TC_M + r]);
       const float tau = tie_tau(x2, v1, cmax, tb);
-      // ---- pass 2: candidates {c < k : v(c) <= tau}, as 32-column bit masks ----
+      // ---- pass 2: this half's candidates {c < k : v(c) <= tau} in ascending order ----
       uint32_t cnt = 0, got = 0, k0 = 0, k1 = 0, k2 = 0, k3 = 0;
-      for (uint32_t pr = 0; pr < npair; ++pr) {
+      for (uint32_t pr = pr0; pr < pr1; ++pr) {
         uint32_t acc[64];
         tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
         tmem_ld_wait();
-        const float4* cn4 = reinterpret_cast<const float4*>(cns + pr * 64u);
+        const float4* cn4 = reinterpret_cast<const float4*>(cn2 + pr * 64u);
         uint32_t mm[2] = {0u, 0u};
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int hh = 0; hh < 2; ++hh) {
 #pragma unroll
           for (int j4 = 0; j4 < 8; ++j4) {
-            const float4 cc = cn4[8 * h + j4];
-            const int a = 32 * h + 4 * j4;
+            const float4 cc = __ldg(cn4 + 8 * hh + j4);
+            const int a = 32 * hh + 4 * j4;
             const float2 va = dist_pair(acc[a + 0], acc[a + 1], cc.x, cc.y);
             const float2 vb = dist_pair(acc[a + 2], acc[a + 3], cc.z, cc.w);
-            mm[h] |= (va.x <= tau ? 1u : 0u) << (4 * j4 + 0);
-            mm[h] |= (va.y <= tau ? 1u : 0u) << (4 * j4 + 1);
-            mm[h] |= (vb.x <= tau ? 1u : 0u) << (4 * j4 + 2);
-            mm[h] |= (vb.y <= tau ? 1u : 0u) << (4 * j4 + 3);
+            mm[hh] |= (va.x <= tau ? 1u : 0u) << (4 * j4 + 0);
+            mm[hh] |= (va.y <= tau ? 1u : 0u) << (4 * j4 + 1);
+            mm[hh] |= (vb.x <= tau ? 1u : 0u) << (4 * j4 + 2);
+            mm[hh] |= (vb.y <= tau ? 1u : 0u) << (4 * j4 + 3);
           }
         }
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const uint32_t c0 = pr * 64u + (uint32_t)h * 32u;
-          uint32_t m = mm[h] & ((c0 >= k) ? 0u : (k - c0 >= 32u ? 0xffffffffu : ((1u << (k - c0)) - 1u)));
+        for (int hh = 0; hh < 2; ++hh) {
+          const uint32_t c0 = pr * 64u + (uint32_t)hh * 32u;
+          uint32_t m = mm[hh] & ((c0 >= k) ? 0u : (k - c0 >= 32u ? 0xffffffffu : ((1u << (k - c0)) - 1u)));
           cnt += (uint32_t)__popc(m);
           while (m != 0u && got < 4u) {
             const uint32_t col = c0 + (uint32_t)(__ffs(m) - 1);
@@ -258,14 +275,41 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
         if (Dout && row < n) {
           for (int j = 0; j < 64; ++j)
             if (pr * 64u + j < k)
-              Dout[row * k + pr * 64u + j] = fmaf(-2.0f, __uint_as_float(acc[j]), cns[pr * 64u + j]) + x2;
+              Dout[row * k + pr * 64u + j] = fmaf(-2.0f, __uint_as_float(acc[j]), __ldg(cn2 + pr * 64u + j)) + x2;
         }
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&ts->tempty[set]);      // accumulator buffer free
-      // Candidates come out in ascending column order: k0 is the lowest index.
-      // NaN anywhere (tau or v1) leaves cnt == 0: such a row takes the full path.
+      if (lane == 0) mbar_arrive(&ts->tempty[buf]);      // this warp is done with the accumulator
+      // The upper half hands its summary to the lower half: min(cnt, 7) and up
+      // to four column offsets (7 bits each, relative to the half's first
+      // column), written to the lower half's exchange slot, which only the
+      // upper half reads and has already read.
+      const uint32_t hbase = nlo * 64u;
+      if (h == 1) {
+        const uint32_t info = min(cnt, 7u) | (((k0 - hbase) & 127u) << 3) | (((k1 - hbase) & 127u) << 10) |
+                              (((k2 - hbase) & 127u) << 17) | (((k3 - hbase) & 127u) << 24);
+        xch[r] = __uint_as_float(info);
+      }
+      if (!pair_sync()) { if (lane == 0) fail(7); break; }
+      if (h == 1) continue;
+      {
+        const uint32_t info = __float_as_uint(xch[r]);
+        const uint32_t cb = info & 7u;
+        // merge: the lower half's candidates come first (lower columns)
+#pragma unroll
+        for (uint32_t i = 0; i < 4; ++i) {
+          if (i < cb && got < 4u) {
+            const uint32_t col = hbase + ((info >> (3 + 7 * i)) & 127u);
+            k0 = (got == 0) ? col : k0; k1 = (got == 1) ? col : k1;
+            k2 = (got == 2) ? col : k2; k3 = (got == 3) ? col : k3;
+            ++got;
+          }
+        }
+        cnt += cb;
+      }
+      // Candidates in ascending column order: k0 is the lowest index.  NaN
+      // anywhere (tau or v1) leaves cnt == 0: such a row takes the full path.
       const bool valid = row < n;
       if (valid) {
         labels[row] = k0;
@@ -645,7 +689,7 @@ TcPlan plan_tc(uint32_t dp, uint32_t kp, int mode, uint64_t n, int num_sms) {
   p.KB = dp / 64;
   const size_t b_bytes = (size_t)p.KB * kp * 128 * (mode != TC_PLAIN ? 2 : 1);
   const size_t unit = (size_t)A_UNIT * (mode == TC_SPLIT3 ? 2 : 1);
-  const size_t fixed = 1024 /*align*/ + ((kp + 63) & ~63u) * 4 + sizeof(TcSmem) + 64;
+  const size_t fixed = 1024 /*align*/ + 2 * TC_M * sizeof(float) /*xch*/ + sizeof(TcSmem) + 64;
   const size_t budget = 227 * 1024;
   if (b_bytes + fixed + 2 * unit > budget) return p;
   size_t s = (budget - b_bytes - fixed) / unit;
