@@ -53,7 +53,9 @@ def peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling every 20 ms around the timed region: sampling has
+    started (first sample read) before the region begins and runs until a
+    sample after its end, so that short regions are bracketed."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -67,10 +69,13 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
+            t0 = time.time()
+            while not self.rows and time.time() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.005)
         except OSError:
             self.proc = None
         return self
@@ -81,6 +86,9 @@ class Clocks:
 
     def __exit__(self, *a):
         if self.proc:
+            n0, t0 = len(self.rows), time.time()
+            while len(self.rows) <= n0 and time.time() - t0 < 1.0 and self.proc.poll() is None:
+                time.sleep(0.005)
             self.proc.terminate()
             try:
                 self.proc.wait(2)
@@ -586,7 +594,9 @@ TRAFFIC = {
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 200 for the lloyd workload, whose iterations take "
+                         "~0.4 ms, so that clock samples fall inside the timed region; 20 otherwise)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16x3", choices=["bf16", "bf16x3", "fp32"])
@@ -597,6 +607,8 @@ def main():
     ap.add_argument("--rows", type=int, default=0,
                     help="bigk only: fewer rows than the workload's n (a smaller case for profilers)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 200 if (args.workload == "lloyd" and args.impl == "ours") else 20
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

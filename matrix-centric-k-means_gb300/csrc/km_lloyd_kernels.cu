@@ -411,15 +411,150 @@ refine_cands_kernel(const float* __restrict__ X, const float* __restrict__ C, ui
     atomicAdd(&st->refined_total, (unsigned long long)block_rows);
 }
 
+// Reference CPU distance as cpu_dist_v4 (same operation order), with the
+// loads arranged for memory-level parallelism: see cpu_dist_v4_mlp.
+__device__ __forceinline__ float4 ldg_nc_v4(const float4* p) {
+  float4 v;
+  asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float cpu_dist_v4_mlp(const float* __restrict__ x, const float* __restrict__ c,
+                                                 uint32_t d) {
+  const float4* x4 = reinterpret_cast<const float4*>(x);
+  const float4* c4 = reinterpret_cast<const float4*>(c);
+  const uint32_t d4 = d / 4;
+  float s = 0.0f;
+  auto step = [&](const float4 a, const float4 b) {
+    float t = __fsub_rn(a.x, b.x); s = __fadd_rn(s, __fmul_rn(t, t));
+    t = __fsub_rn(a.y, b.y); s = __fadd_rn(s, __fmul_rn(t, t));
+    t = __fsub_rn(a.z, b.z); s = __fadd_rn(s, __fmul_rn(t, t));
+    t = __fsub_rn(a.w, b.w); s = __fadd_rn(s, __fmul_rn(t, t));
+  };
+  // Groups of four 128-byte lines of each row: the first 16 bytes of all eight
+  // lines are loaded together (eight misses in flight), so the rest of each
+  // line is already in L1 when the ordered chain reaches it.
+  uint32_t q = 0;
+  for (; q + 32 <= d4; q += 32) {
+    float4 a[4], b[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { a[i] = ldg_nc_v4(x4 + q + 8 * i); b[i] = ldg_nc_v4(c4 + q + 8 * i); }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      step(a[i], b[i]);
+      float4 ra[7], rb[7];
+#pragma unroll
+      for (int r = 0; r < 7; ++r) { ra[r] = __ldg(x4 + q + 8 * i + 1 + r); rb[r] = __ldg(c4 + q + 8 * i + 1 + r); }
+#pragma unroll
+      for (int r = 0; r < 7; ++r) step(ra[r], rb[r]);
+    }
+  }
+  for (; q < d4; ++q) step(x4[q], c4[q]);
+  return s;
+}
+
+// The same re-score with the (row, candidate) pairs packed one per lane
+// (d % 4 == 0, 16-byte aligned rows): a warp takes RP_SEGS queue segments,
+// lane e loads entry e, a warp prefix over the candidate counts places pair
+// (e, m) on lane off[e] + m, every lane runs one exact chain, and lane e picks
+// its row's minimum (candidates are in ascending index order, so a strict '<'
+// keeps the lowest index on ties).  With 2..4 candidates per row and a few
+// rows per segment, four lanes per row left most lanes idle.
+constexpr int RP_SEGS = 4;
+
+__global__ void __launch_bounds__(32 * RC_WARPS, 2)
+refine_pairs_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
+                    DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
+                    float* __restrict__ mindist, bool count) {
+  if (st->done) return;
+  __shared__ float sv[RC_WARPS][32][4];
+  __shared__ uint32_t block_rows;
+  if (threadIdx.x == 0) block_rows = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t seg0 = warp * RP_SEGS;
+  const uint32_t c = (lane < RP_SEGS && seg0 + (uint64_t)lane < rq.nseg) ? rq.ccnt[seg0 + lane] : 0u;
+  uint32_t pre[RP_SEGS];
+  uint32_t run = 0;
+#pragma unroll
+  for (int q = 0; q < RP_SEGS; ++q) {
+    run += __shfl_sync(0xffffffffu, c, q);
+    pre[q] = run;
+  }
+  const uint32_t total = run;
+  for (uint32_t e0 = 0; e0 < total; e0 += 32) {
+    const uint32_t qi = e0 + (uint32_t)lane;
+    const bool has = qi < total;
+    RefineEntry en{0u, 0u, {0u, 0u, 0u, 0u}};
+    if (has) {
+      uint32_t sg = 0, before = 0;
+#pragma unroll
+      for (int q = 0; q < RP_SEGS - 1; ++q)
+        if (qi >= pre[q]) { sg = (uint32_t)q + 1u; before = pre[q]; }
+      en = rq.cand[(seg0 + sg) * 32 + (qi - before)];
+    }
+    const uint32_t cl = has ? min(en.cnt, 4u) : 0u;
+    // exclusive prefix of the candidate counts over the lanes
+    uint32_t incl = cl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const uint32_t off = incl - cl;
+    const uint32_t npairs = __shfl_sync(0xffffffffu, incl, 31);
+    for (uint32_t p0 = 0; p0 < npairs; p0 += 32) {
+      const uint32_t p = p0 + (uint32_t)lane;
+      // owner: the last lane whose offset is <= p
+      uint32_t e = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const uint32_t cand = e + (uint32_t)step;
+        const uint32_t oc = __shfl_sync(0xffffffffu, off, (int)(cand & 31u));
+        if (cand < 32u && oc <= p) e = cand;
+      }
+      const uint32_t m = p - __shfl_sync(0xffffffffu, off, (int)e);
+      const uint32_t row = __shfl_sync(0xffffffffu, en.row, (int)e);
+      const uint32_t c0 = __shfl_sync(0xffffffffu, en.c[0], (int)e);
+      const uint32_t c1 = __shfl_sync(0xffffffffu, en.c[1], (int)e);
+      const uint32_t c2 = __shfl_sync(0xffffffffu, en.c[2], (int)e);
+      const uint32_t c3 = __shfl_sync(0xffffffffu, en.c[3], (int)e);
+      if (p < npairs) {
+        const uint32_t cc = m == 0 ? c0 : m == 1 ? c1 : m == 2 ? c2 : c3;
+        sv[wib][e][m & 3u] = cpu_dist_v4_mlp(X + (uint64_t)row * d, C + (uint64_t)cc * d, d);
+      }
+    }
+    __syncwarp();
+    if (has) {
+      float bv = sv[wib][lane][0];
+      uint32_t bi = en.c[0];
+#pragma unroll
+      for (uint32_t m = 1; m < 4; ++m)
+        if (m < cl && sv[wib][lane][m] < bv) { bv = sv[wib][lane][m]; bi = en.c[m]; }
+      labels[en.row] = bi;
+      if (mindist) mindist[en.row] = bv;
+    }
+    __syncwarp();
+  }
+  if (count && lane == 0 && total) atomicAdd(&block_rows, total);
+  __syncthreads();
+  if (count && threadIdx.x == 0 && block_rows)
+    atomicAdd(&st->refined_total, (unsigned long long)block_rows);
+}
+
 static void launch_refine_cands(bool v4, const float* X, const float* C, uint32_t d, DevState* st,
                                 const RefineQueues& rq, uint32_t* labels, float* mindist, bool count,
                                 cudaStream_t s) {
-  const uint64_t warps = (rq.nseg + RC_SEGS - 1) / RC_SEGS;
-  const unsigned blocks = (unsigned)std::max<uint64_t>(1, (warps + RC_WARPS - 1) / RC_WARPS);
-  if (v4)
-    refine_cands_kernel<true><<<blocks, 32 * RC_WARPS, 0, s>>>(X, C, d, st, rq, labels, mindist, count);
-  else
+  if (v4) {
+    const uint64_t warps = (rq.nseg + RP_SEGS - 1) / RP_SEGS;
+    const unsigned blocks = (unsigned)std::max<uint64_t>(1, (warps + RC_WARPS - 1) / RC_WARPS);
+    refine_pairs_kernel<<<blocks, 32 * RC_WARPS, 0, s>>>(X, C, d, st, rq, labels, mindist, count);
+  } else {
+    const uint64_t warps = (rq.nseg + RC_SEGS - 1) / RC_SEGS;
+    const unsigned blocks = (unsigned)std::max<uint64_t>(1, (warps + RC_WARPS - 1) / RC_WARPS);
     refine_cands_kernel<false><<<blocks, 32 * RC_WARPS, 0, s>>>(X, C, d, st, rq, labels, mindist, count);
+  }
 }
 
 // Exact re-score against all k centroids: one warp per group of up to four
@@ -545,7 +680,7 @@ __global__ void full_compact_kernel(DevState* st, RefineQueues rq, uint32_t* __r
 // warp per row, lanes stride over the row's candidates, the reference's CPU
 // distance; smallest distance wins, lowest index on ties.
 template <bool V4>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 refine_wide_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
                    DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
                    float* __restrict__ mindist) {
@@ -566,7 +701,7 @@ refine_wide_kernel(const float* __restrict__ X, const float* __restrict__ C, uin
       for (uint32_t e = (uint32_t)lane; e < nc; e += 32u) {
         const uint32_t c = rq.wl[(uint64_t)row * rq.L + e].x;
         const float* cc = C + (uint64_t)c * d;
-        const float v = V4 ? cpu_dist_v4(x, cc, d) : cpu_dist(x, cc, d);
+        const float v = V4 ? cpu_dist_v4_mlp(x, cc, d) : cpu_dist(x, cc, d);
         if (v < bv || (v == bv && c < bi)) { bv = v; bi = c; }
       }
       for (int o = 16; o > 0; o >>= 1) {

@@ -213,26 +213,25 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       tc_fence_after();
       const uint32_t tbase = tmem_base + (((uint32_t)q * 32u) << 16) + buf * nalloc;
       // ---- pass 1: partial row minimum of v = ||c||^2 - 2 acc over this half ----
-      float m0 = __int_as_float(0x7f800000), m1 = m0, m2 = m0, m3 = m0;
+      // eight independent min chains (four steps per 64 columns each)
+      float mv[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) mv[i] = __int_as_float(0x7f800000);
       for (uint32_t pr = pr0; pr < pr1; ++pr) {
         uint32_t acc[64];
         tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
         tmem_ld_wait();
         const float4* cn4 = reinterpret_cast<const float4*>(cn2 + pr * 64u);
 #pragma unroll
-        for (int j4 = 0; j4 < 16; j4 += 2) {
-          const float4 ca = __ldg(cn4 + j4), cb = __ldg(cn4 + j4 + 1);
-          const float2 va = dist_pair(acc[4 * j4 + 0], acc[4 * j4 + 1], ca.x, ca.y);
-          const float2 vb = dist_pair(acc[4 * j4 + 2], acc[4 * j4 + 3], ca.z, ca.w);
-          const float2 vc = dist_pair(acc[4 * j4 + 4], acc[4 * j4 + 5], cb.x, cb.y);
-          const float2 vd = dist_pair(acc[4 * j4 + 6], acc[4 * j4 + 7], cb.z, cb.w);
-          m0 = fmin3(m0, va.x, va.y);
-          m1 = fmin3(m1, vb.x, vb.y);
-          m2 = fmin3(m2, vc.x, vc.y);
-          m3 = fmin3(m3, vd.x, vd.y);
+        for (int j4 = 0; j4 < 16; ++j4) {
+          const float4 cc = __ldg(cn4 + j4);
+          const float2 va = dist_pair(acc[4 * j4 + 0], acc[4 * j4 + 1], cc.x, cc.y);
+          const float2 vb = dist_pair(acc[4 * j4 + 2], acc[4 * j4 + 3], cc.z, cc.w);
+          mv[(2 * j4) & 7] = fmin3(mv[(2 * j4) & 7], va.x, va.y);
+          mv[(2 * j4 + 1) & 7] = fmin3(mv[(2 * j4 + 1) & 7], vb.x, vb.y);
         }
       }
-      const float mh = fmin3(m0, m1, fminf(m2, m3));
+      const float mh = fminf(fmin3(mv[0], mv[1], mv[2]), fmin3(mv[3], mv[4], fmin3(mv[5], mv[6], mv[7])));
       xch[h * TC_M + r] = mh;
       if (!pair_sync()) { if (lane == 0) fail(6); break; }
       const float v1 = fminf(mh, xch[(1 - h) * TC_M + r]);
@@ -244,20 +243,23 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
         tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
         tmem_ld_wait();
         const float4* cn4 = reinterpret_cast<const float4*>(cn2 + pr * 64u);
-        uint32_t mm[2] = {0u, 0u};
+        uint32_t mm[2];
 #pragma unroll
         for (int hh = 0; hh < 2; ++hh) {
+          // four independent partial masks, one per column residue mod 4
+          uint32_t q0 = 0u, q1 = 0u, q2 = 0u, q3 = 0u;
 #pragma unroll
           for (int j4 = 0; j4 < 8; ++j4) {
             const float4 cc = __ldg(cn4 + 8 * hh + j4);
             const int a = 32 * hh + 4 * j4;
             const float2 va = dist_pair(acc[a + 0], acc[a + 1], cc.x, cc.y);
             const float2 vb = dist_pair(acc[a + 2], acc[a + 3], cc.z, cc.w);
-            mm[hh] |= (va.x <= tau ? 1u : 0u) << (4 * j4 + 0);
-            mm[hh] |= (va.y <= tau ? 1u : 0u) << (4 * j4 + 1);
-            mm[hh] |= (vb.x <= tau ? 1u : 0u) << (4 * j4 + 2);
-            mm[hh] |= (vb.y <= tau ? 1u : 0u) << (4 * j4 + 3);
+            q0 |= (va.x <= tau ? 1u : 0u) << (4 * j4 + 0);
+            q1 |= (va.y <= tau ? 1u : 0u) << (4 * j4 + 1);
+            q2 |= (vb.x <= tau ? 1u : 0u) << (4 * j4 + 2);
+            q3 |= (vb.y <= tau ? 1u : 0u) << (4 * j4 + 3);
           }
+          mm[hh] = (q0 | q1) | (q2 | q3);
         }
 #pragma unroll
         for (int hh = 0; hh < 2; ++hh) {
