@@ -323,8 +323,7 @@ km_status LloydEngine::enqueue_assign(float* Dout) {
 km_status LloydEngine::enqueue_finalize(const LoopConsts& lc) {
   finalize_kernel<<<(k * 32 + 255) / 256, 256, 0, stream>>>(Cn, C, dsq, objpart, counts, lc.empty, d, dp, k,
                                                             lc.tol, cn2,
-                                                            Cb, Clo, Ct, shift_c, obj_c, st);
-  control_kernel<<<1, 256, 0, stream>>>(cn2, shift_c, obj_c, k, lc, st);
+                                                            Cb, Clo, Ct, shift_c, obj_c, st, lc);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }

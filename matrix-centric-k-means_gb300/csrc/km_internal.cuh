@@ -44,7 +44,7 @@ struct DevState {
   uint32_t x_not_bf16;      // set_data: some coordinate is not exactly a BF16 value
   uint32_t err;             // device error bits (KM_DEVERR_*)
   uint32_t err_where;       // first wait that ran out (diagnostics)
-  uint32_t pad3;
+  uint32_t fin_ticket;       // finalize blocks done in this iteration (the last one resets it)
   unsigned long long refined_total;  // rows re-scored (all iterations)
   unsigned long long full_total;     // of those, against all k centroids
   float cmax;               // max_c ||c|| of the centroids the next assignment uses

@@ -45,9 +45,7 @@ __global__ void finalize_kernel(const float* Cn, float* C, const float* dsq, con
                                 const uint32_t* counts, int32_t empty_excl,
                                 uint32_t d, uint32_t dp, uint32_t k, float tol, float* cn2,
                                 __nv_bfloat16* Cb, __nv_bfloat16* Clo, float* Ct,
-                                double* shift_c, double* obj_c, DevState* st);
-__global__ void control_kernel(const float* cn2, const double* shift_c, const double* obj_c,
-                               uint32_t k, LoopConsts lc, DevState* st);
+                                double* shift_c, double* obj_c, DevState* st, LoopConsts lc);
 
 // ---- tensor-core distance stage (km_tc.cu) ----
 struct TcPlan {

@@ -575,14 +575,16 @@ refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, ui
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   uint32_t done_rows = 0;
-  // 32 segment counts per load; only the non-empty segments are visited
-  for (uint64_t g0 = warp * 32; g0 < rq.nseg; g0 += nw * 32) {
-   const uint32_t cl = (g0 + (uint64_t)lane < rq.nseg) ? rq.fcnt[g0 + lane] : 0u;
+  // Segments warp, warp + nw, warp + 2 nw, ... (a dense queue spreads over all
+  // warps); 32 of their counts per load, only the non-empty ones visited.
+  for (uint64_t g0 = warp; g0 < rq.nseg; g0 += nw * 32) {
+   const uint64_t sgl = g0 + (uint64_t)lane * nw;
+   const uint32_t cl = (sgl < rq.nseg) ? rq.fcnt[sgl] : 0u;
    uint32_t nz = __ballot_sync(0xffffffffu, cl != 0u);
    while (nz) {
    const int sl = __ffs(nz) - 1;
    nz &= nz - 1u;
-   const uint64_t seg = g0 + (uint64_t)sl;
+   const uint64_t seg = g0 + (uint64_t)sl * nw;
    const uint32_t cnt = __shfl_sync(0xffffffffu, cl, sl);
    done_rows += cnt;
    for (uint32_t e0 = 0; e0 < cnt; e0 += FULL_ROWS) {
@@ -1286,79 +1288,94 @@ km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_
 // One warp per cluster: reference shift test (float sum over j ascending, then
 // sqrtf(s) > tol, kmeans.cpp:190-200), FP64 move, FP64 objective of the
 // cluster, new ||c||^2 and BF16 copies; then C <- Cn.
-__global__ void finalize_kernel(const float* __restrict__ Cn, float* __restrict__ C,
-                                const float* __restrict__ dsq, const double* __restrict__ objpart,
-                                const uint32_t* __restrict__ counts, int32_t empty_excl,
-                                uint32_t d, uint32_t dp, uint32_t k, float tol,
-                                float* __restrict__ cn2, __nv_bfloat16* __restrict__ Cb,
-                                __nv_bfloat16* __restrict__ Clo, float* __restrict__ Ct,
-                                double* __restrict__ shift_c, double* __restrict__ obj_c,
-                                DevState* st) {
+// One warp per cluster: reference shift test (float sum over j ascending, then
+// sqrtf(s) > tol, kmeans.cpp:190-200), FP64 move, FP64 objective of the
+// cluster, new ||c||^2 and BF16 copies; then C <- Cn.  The block that finishes
+// last (a ticket in DevState) then ends the iteration: deterministic
+// reductions over the clusters, the stop decision, counters for the next
+// iteration.
+__global__ void __launch_bounds__(256)
+finalize_kernel(const float* __restrict__ Cn, float* __restrict__ C,
+                const float* __restrict__ dsq, const double* __restrict__ objpart,
+                const uint32_t* __restrict__ counts, int32_t empty_excl,
+                uint32_t d, uint32_t dp, uint32_t k, float tol,
+                float* __restrict__ cn2, __nv_bfloat16* __restrict__ Cb,
+                __nv_bfloat16* __restrict__ Clo, float* __restrict__ Ct,
+                double* __restrict__ shift_c, double* __restrict__ obj_c,
+                DevState* st, LoopConsts lc) {
   if (st->done) return;
-  const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (c >= k) return;
-  const uint64_t base = (uint64_t)c * d;
-  // Reference GPU rule (src/kernels/distances.cu:588-599): an empty cluster's
-  // distance is +inf from then on, so it is never chosen again.  Its norm and
-  // its column of Ct become +inf; its (zero) centroid row stays finite.
-  const bool excl = empty_excl && counts[c] == 0u;
-  double nrm = 0.0, mv = 0.0, ob = 0.0;
-  for (uint32_t j = lane; j < dp; j += 32) {
-    const float v = (j < d) ? Cn[base + j] : 0.0f;
-    if (j < d) {
-      nrm += (double)v * v;
-      const double t = (double)v - (double)C[base + j];
-      mv += t * t;
-      ob += objpart[base + j];
-      Ct[(uint64_t)j * k + c] = excl ? f_inf() : v;
-    }
-    if (Cb) {
-      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-      Cb[(uint64_t)c * dp + j] = hi;
-      if (Clo) Clo[(uint64_t)c * dp + j] = __float2bfloat16_rn(v - __bfloat162float(hi));
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
-    mv += __shfl_xor_sync(0xffffffffu, mv, o);
-    ob += __shfl_xor_sync(0xffffffffu, ob, o);
-  }
-  // Reference shift test: float sum over j ascending.  Coalesced loads of 32
-  // terms, each broadcast in order into the same chain on every lane.
-  float s = 0.0f;
-  for (uint32_t j0 = 0; j0 < d; j0 += 32) {
-    const float t = (j0 + (uint32_t)lane < d) ? dsq[base + j0 + lane] : 0.0f;
-    const uint32_t m = min(32u, d - j0);
-    for (uint32_t q = 0; q < m; ++q) s = __fadd_rn(s, __shfl_sync(0xffffffffu, t, (int)q));
-  }
-  if (lane == 0) {
-    if (sqrtf(s) > tol) st->moved = 1u;
-    cn2[c] = excl ? f_inf() : (float)nrm;
-    shift_c[c] = sqrt(mv);
-    obj_c[c] = ob;
-  }
-  __syncwarp();
-  for (uint32_t j = lane; j < d; j += 32) C[base + j] = Cn[base + j];
-}
-
-// Single block: end of iteration.  Deterministic reductions over clusters,
-// stop decision, counters for the next iteration.
-__global__ void control_kernel(const float* __restrict__ cn2, const double* __restrict__ shift_c,
-                               const double* __restrict__ obj_c, uint32_t k, LoopConsts lc,
-                               DevState* st) {
-  if (st->done) return;
+  __shared__ float sterm[8][32];
   __shared__ double s_obj[256];
   __shared__ double s_sh[256];
   __shared__ float s_cm[256];
+  __shared__ int is_last;
+  const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  if (c < k) {
+    const uint64_t base = (uint64_t)c * d;
+    // Reference GPU rule (src/kernels/distances.cu:588-599): an empty cluster's
+    // distance is +inf from then on, so it is never chosen again.  Its norm and
+    // its column of Ct become +inf; its (zero) centroid row stays finite.
+    const bool excl = empty_excl && counts[c] == 0u;
+    double nrm = 0.0, mv = 0.0, ob = 0.0;
+    for (uint32_t j = lane; j < dp; j += 32) {
+      const float v = (j < d) ? Cn[base + j] : 0.0f;
+      if (j < d) {
+        nrm += (double)v * v;
+        const double t = (double)v - (double)C[base + j];
+        mv += t * t;
+        ob += objpart[base + j];
+        Ct[(uint64_t)j * k + c] = excl ? f_inf() : v;
+      }
+      if (Cb) {
+        const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+        Cb[(uint64_t)c * dp + j] = hi;
+        if (Clo) Clo[(uint64_t)c * dp + j] = __float2bfloat16_rn(v - __bfloat162float(hi));
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
+      mv += __shfl_xor_sync(0xffffffffu, mv, o);
+      ob += __shfl_xor_sync(0xffffffffu, ob, o);
+    }
+    // Reference shift test: float sum over j ascending.  Coalesced loads of 32
+    // terms into shared memory, summed in order by lane 0.
+    float s = 0.0f;
+    for (uint32_t j0 = 0; j0 < d; j0 += 32) {
+      sterm[wib][lane] = (j0 + (uint32_t)lane < d) ? dsq[base + j0 + lane] : 0.0f;
+      __syncwarp();
+      if (lane == 0) {
+        const uint32_t m = min(32u, d - j0);
+        for (uint32_t q = 0; q < m; ++q) s = __fadd_rn(s, sterm[wib][q]);
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      if (sqrtf(s) > tol) st->moved = 1u;
+      cn2[c] = excl ? f_inf() : (float)nrm;
+      shift_c[c] = sqrt(mv);
+      obj_c[c] = ob;
+    }
+    __syncwarp();
+    for (uint32_t j = lane; j < d; j += 32) C[base + j] = Cn[base + j];
+  }
+  // ---- last block: end of iteration ----
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = (atomicAdd(&st->fin_ticket, 1u) == gridDim.x - 1u) ? 1 : 0;
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  // other blocks' results: read past L1 (this SM may hold stale lines)
+  volatile DevState* vs = st;
   double ob = 0.0, sh = 0.0;
   float cm = 0.0f;
   const uint32_t per = (k + blockDim.x - 1) / blockDim.x;
   const uint32_t b = threadIdx.x * per, e = min(k, b + per);
-  for (uint32_t c = b; c < e; ++c) {
-    ob += obj_c[c];
-    sh = fmax(sh, shift_c[c]);
-    const float v = cn2[c];
+  for (uint32_t cc = b; cc < e; ++cc) {
+    ob += __ldcg(obj_c + cc);
+    sh = fmax(sh, __ldcg(shift_c + cc));
+    const float v = __ldcg(cn2 + cc);
     if (v < f_inf()) cm = fmaxf(cm, sqrtf(v));   // excluded (empty) clusters hold +inf
   }
   s_obj[threadIdx.x] = ob; s_sh[threadIdx.x] = sh; s_cm[threadIdx.x] = cm;
@@ -1372,25 +1389,26 @@ __global__ void control_kernel(const float* __restrict__ cn2, const double* __re
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const uint32_t it = st->iter + 1;
-    st->iter = it;
-    st->objective = s_obj[0];
-    st->max_shift = s_sh[0];
-    st->cmax = s_cm[0] * 1.000001f;
-    const double score = s_obj[0] - st->sum_x2;
-    st->score = score;
+    const uint32_t it = vs->iter + 1;
+    vs->iter = it;
+    vs->objective = s_obj[0];
+    vs->max_shift = s_sh[0];
+    vs->cmax = s_cm[0] * 1.000001f;
+    const double score = s_obj[0] - vs->sum_x2;
+    vs->score = score;
     bool stop = false;
     if (lc.conv == KM_CONV_SHIFT) {
-      if (it > 1 && st->moved == 0u) { st->converged_iter = it; stop = true; }
+      if (it > 1 && vs->moved == 0u) { vs->converged_iter = it; stop = true; }
     } else if (lc.conv == KM_CONV_SCORE) {
-      if (it < lc.maxiter && it > 1 && fabs(score - st->last_score) < (double)lc.tol) {
-        st->converged_iter = it; stop = true;
+      if (it < lc.maxiter && it > 1 && fabs(score - vs->last_score) < (double)lc.tol) {
+        vs->converged_iter = it; stop = true;
       }
-      st->last_score = score;
+      vs->last_score = score;
     }
-    st->moved = 0u;
+    vs->moved = 0u;
     if (it >= lc.maxiter) stop = true;
-    if (stop) st->done = 1u;
+    if (stop) vs->done = 1u;
+    vs->fin_ticket = 0u;
   }
 }
 
