@@ -314,44 +314,17 @@ km_status launch_assign_f32(const float* X, const float* C, const float* cn2, co
   return KM_OK;
 }
 
-// Reference CPU distance of one row to one centroid with 16-byte loads (d % 4
-// == 0 and 16-byte aligned rows); the operation order is unchanged.
-__device__ __forceinline__ float cpu_dist_v4(const float* __restrict__ x, const float* __restrict__ c,
-                                             uint32_t d) {
-  const float4* x4 = reinterpret_cast<const float4*>(x);
-  const float4* c4 = reinterpret_cast<const float4*>(c);
-  const uint32_t d4 = d / 4;
-  float s = 0.0f;
-  auto step = [&](const float4 a, const float4 b) {
-    float t = __fsub_rn(a.x, b.x); s = __fadd_rn(s, __fmul_rn(t, t));
-    t = __fsub_rn(a.y, b.y); s = __fadd_rn(s, __fmul_rn(t, t));
-    t = __fsub_rn(a.z, b.z); s = __fadd_rn(s, __fmul_rn(t, t));
-    t = __fsub_rn(a.w, b.w); s = __fadd_rn(s, __fmul_rn(t, t));
-  };
-  uint32_t q = 0;
-  // eight 16-byte loads of each row in flight before the ordered chain uses them
-  for (; q + 8 <= d4; q += 8) {
-    float4 a[8], b[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) { a[i] = x4[q + i]; b[i] = c4[q + i]; }
-#pragma unroll
-    for (int i = 0; i < 8; ++i) step(a[i], b[i]);
-  }
-  for (; q < d4; ++q) step(x4[q], c4[q]);
-  return s;
-}
-
-// Exact re-score of rows with 2..4 candidates: four lanes per row, one
-// candidate per lane, the reference's CPU distance (float, j ascending);
-// smallest distance wins, lowest index on ties.  The candidate set provably
-// holds the reference argmin over all k (tie_tau / tie_class).
+// Exact re-score of rows with 2..4 candidates, for rows that are not 16-byte
+// aligned or d % 4 != 0 (refine_pairs_kernel below is the vector path): four
+// lanes per row, one candidate per lane, the reference's CPU distance (float,
+// j ascending); smallest distance wins, lowest index on ties.  The candidate
+// set provably holds the reference argmin over all k (tie_tau / tie_class).
 // One warp per RC_SEGS consecutive queue segments, their entries flattened so
 // that every pass keeps eight rows in flight; the grid covers all segments at
 // once (no loop over segments, so a warp pays one count load and its rows).
 constexpr int RC_SEGS = 2;
 constexpr int RC_WARPS = 8;
 
-template <bool V4>
 __global__ void __launch_bounds__(32 * RC_WARPS)
 refine_cands_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
                     DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
@@ -390,7 +363,7 @@ refine_cands_kernel(const float* __restrict__ X, const float* __restrict__ C, ui
         const uint32_t cc = en.c[slot];
         const float* x = X + (uint64_t)row * d;
         const float* cr = C + (uint64_t)cc * d;
-        const float v = V4 ? cpu_dist_v4(x, cr, d) : cpu_dist(x, cr, d);
+        const float v = cpu_dist(x, cr, d);
         if (v < bv) { bv = v; bi = cc; }
       }
     }
@@ -411,15 +384,16 @@ refine_cands_kernel(const float* __restrict__ X, const float* __restrict__ C, ui
     atomicAdd(&st->refined_total, (unsigned long long)block_rows);
 }
 
-// Reference CPU distance as cpu_dist_v4 (same operation order), with the
-// loads arranged for memory-level parallelism: see cpu_dist_v4_mlp.
+// Reference CPU distance with 16-byte loads (d % 4 == 0 and 16-byte aligned
+// rows): the operation order of cpu_dist, the loads arranged for memory-level
+// parallelism (below).
 __device__ __forceinline__ float4 ldg_nc_v4(const float4* p) {
   float4 v;
   asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
                : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
   return v;
 }
-__device__ __forceinline__ float cpu_dist_v4_mlp(const float* __restrict__ x, const float* __restrict__ c,
+__device__ __forceinline__ float cpu_dist_v4(const float* __restrict__ x, const float* __restrict__ c,
                                                  uint32_t d) {
   const float4* x4 = reinterpret_cast<const float4*>(x);
   const float4* c4 = reinterpret_cast<const float4*>(c);
@@ -522,7 +496,7 @@ refine_pairs_kernel(const float* __restrict__ X, const float* __restrict__ C, ui
       const uint32_t c3 = __shfl_sync(0xffffffffu, en.c[3], (int)e);
       if (p < npairs) {
         const uint32_t cc = m == 0 ? c0 : m == 1 ? c1 : m == 2 ? c2 : c3;
-        sv[wib][e][m & 3u] = cpu_dist_v4_mlp(X + (uint64_t)row * d, C + (uint64_t)cc * d, d);
+        sv[wib][e][m & 3u] = cpu_dist_v4(X + (uint64_t)row * d, C + (uint64_t)cc * d, d);
       }
     }
     __syncwarp();
@@ -553,7 +527,7 @@ static void launch_refine_cands(bool v4, const float* X, const float* C, uint32_
   } else {
     const uint64_t warps = (rq.nseg + RC_SEGS - 1) / RC_SEGS;
     const unsigned blocks = (unsigned)std::max<uint64_t>(1, (warps + RC_WARPS - 1) / RC_WARPS);
-    refine_cands_kernel<false><<<blocks, 32 * RC_WARPS, 0, s>>>(X, C, d, st, rq, labels, mindist, count);
+    refine_cands_kernel<<<blocks, 32 * RC_WARPS, 0, s>>>(X, C, d, st, rq, labels, mindist, count);
   }
 }
 
@@ -703,7 +677,7 @@ refine_wide_kernel(const float* __restrict__ X, const float* __restrict__ C, uin
       for (uint32_t e = (uint32_t)lane; e < nc; e += 32u) {
         const uint32_t c = rq.wl[(uint64_t)row * rq.L + e].x;
         const float* cc = C + (uint64_t)c * d;
-        const float v = V4 ? cpu_dist_v4_mlp(x, cc, d) : cpu_dist(x, cc, d);
+        const float v = V4 ? cpu_dist_v4(x, cc, d) : cpu_dist(x, cc, d);
         if (v < bv || (v == bv && c < bi)) { bv = v; bi = c; }
       }
       for (int o = 16; o > 0; o >>= 1) {

@@ -238,10 +238,18 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       const float tau = tie_tau(x2, v1, cmax, tb);
       // ---- pass 2: this half's candidates {c < k : v(c) <= tau} in ascending order ----
       uint32_t cnt = 0, got = 0, k0 = 0, k1 = 0, k2 = 0, k3 = 0;
+      bool released = false;
       for (uint32_t pr = pr0; pr < pr1; ++pr) {
         uint32_t acc[64];
         tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
         tmem_ld_wait();
+        if (pr + 1 == pr1) {
+          // the last load of this tile has landed: the accumulator is free
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&ts->tempty[buf]);
+          released = true;
+        }
         const float4* cn4 = reinterpret_cast<const float4*>(cn2 + pr * 64u);
         uint32_t mm[2];
 #pragma unroll
@@ -280,9 +288,11 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
               Dout[row * k + pr * 64u + j] = fmaf(-2.0f, __uint_as_float(acc[j]), __ldg(cn2 + pr * 64u + j)) + x2;
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&ts->tempty[buf]);      // this warp is done with the accumulator
+      if (!released) {                                   // this half had no columns
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&ts->tempty[buf]);
+      }
       // The upper half hands its summary to the lower half: min(cnt, 7) and up
       // to four column offsets (7 bits each, relative to the half's first
       // column), written to the lower half's exchange slot, which only the
