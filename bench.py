@@ -355,6 +355,26 @@ def _event_ms(fn, stream):
     return e0.elapsed_time(e1), out
 
 
+def stages_only(args):
+    """Per-stage times of the lloyd workload on one GPU: a 5-iteration fit
+    (graph built, warm) then Lloyd.profile(10)."""
+    import torch
+    import helpers
+    km = helpers.km()
+    X = make_data(km)
+    Xd = torch.from_numpy(X).cuda()
+    stream = torch.cuda.Stream()
+    names = ["distance+argmin", "refine", "label sort", "centroid sums", "finalize+control"]
+    with torch.cuda.stream(stream):
+        m = km.Lloyd(N, D, K, tol=TOL, seed=KM_SEED, maxiter=5, precision=args.precision, conv="none",
+                     stream=stream.cuda_stream).set_data(Xd)
+        m.fit(want_centroids=False)
+        st = m.profile(10)
+        m.close()
+    return {"workload": bench_config(1)["workload"], "precision": args.precision,
+            "stages_ms": dict(zip(names, st))}
+
+
 def bigk_arm(args):
     """Lloyd with n = 4,194,304, d = 256, k = 4096, BF16-stored points from a
     seeded mixture with Zipf(1.1) cluster sizes, per-cluster sigma U[0.2, 2],
@@ -637,6 +657,9 @@ def main():
                     help="lloyd: the headline n=1M d=128 k=256 workload (default); bigk: n=4M d=256 "
                          "k=4096 BF16 points; kkm: kernel k-means n=65536 d=512 k=64; batch: 512 "
                          "uneven problems x 8 restarts in one launch")
+    ap.add_argument("--stages-only", action="store_true",
+                    help="lloyd only: a 5-iteration fit and the per-stage timer (Lloyd.profile) of "
+                         "--precision, printed as one JSON line (a short command for profilers)")
     ap.add_argument("--rows", type=int, default=0,
                     help="bigk only: fewer rows than the workload's n (a smaller case for profilers)")
     args = ap.parse_args()
@@ -649,6 +672,9 @@ def main():
         line = reference_arm(args, rank)
         if line is not None:
             print(json.dumps(line), flush=True)
+        return
+    if args.stages_only:
+        print(json.dumps(stages_only(args)), flush=True)
         return
     if args.workload != "lloyd":
         if rank == 0:
