@@ -540,7 +540,7 @@ static void launch_refine_cands(bool v4, const float* X, const float* C, uint32_
 // argmin (kmeans.cpp:106-122).
 constexpr int FULL_ROWS = 4;
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, uint32_t d, uint32_t k,
                    DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
                    float* __restrict__ mindist, bool count) {
@@ -580,18 +580,29 @@ refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, ui
       for (int r = 0; r < FULL_ROWS; ++r)
 #pragma unroll
         for (int t = 0; t < 8; ++t) s[r][t] = 0.0f;
-      for (uint32_t j = 0; j < d; ++j) {
-        float xj[FULL_ROWS];
+      // Four j steps per group: all their loads (the rows' x_j, the lanes'
+      // centroid columns from Ct) are issued before the group's arithmetic,
+      // which keeps 48 loads in flight per lane instead of one step's.
+      for (uint32_t j0 = 0; j0 < d; j0 += 4) {
+        float xj[4][FULL_ROWS], cv[4][8];
 #pragma unroll
-        for (int r = 0; r < FULL_ROWS; ++r) xj[r] = x[r][j];
-        const float* ct = Ct + (uint64_t)j * k + cb + lane;
+        for (int q = 0; q < 4; ++q) {
+          const uint32_t j = j0 + (uint32_t)q;
+          const bool jin = j < d;
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-          if (cb + lane + 32 * t < k) {
-            const float cv = ct[32 * t];
+          for (int r = 0; r < FULL_ROWS; ++r) xj[q][r] = jin ? x[r][j] : 0.0f;
+          const float* ct = Ct + (uint64_t)(jin ? j : 0u) * k + cb + lane;
+#pragma unroll
+          for (int t = 0; t < 8; ++t) cv[q][t] = (jin && cb + lane + 32 * t < k) ? ct[32 * t] : 0.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (j0 + (uint32_t)q >= d) break;
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
 #pragma unroll
             for (int r = 0; r < FULL_ROWS; ++r) {
-              const float tt = __fsub_rn(xj[r], cv);
+              const float tt = __fsub_rn(xj[q][r], cv[q][t]);
               s[r][t] = __fadd_rn(s[r][t], __fmul_rn(tt, tt));
             }
           }
