@@ -62,7 +62,8 @@ enum : uint32_t {
   KM_DEVERR_OVERFLOW = 4u   // refinement list overflow (cannot happen: list holds n)
 };
 
-// Per-fit constants passed by value to the control kernel.
+// Per-fit constants passed by value to the kernels that end an iteration
+// (finalize_kernel, kkm_control_kernel).
 struct LoopConsts {
   uint64_t maxiter;
   float tol;

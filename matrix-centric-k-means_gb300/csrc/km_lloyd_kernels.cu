@@ -1,7 +1,8 @@
 // Lloyd k-means kernels for sm_103a: point/centroid preparation, the SIMT FP32
 // distance stage with fused top-3 argmin, exact near-tie refinement, the
 // stable label sort (one-hot V as a label-sorted permutation), the exact
-// centroid update V.X, and the per-iteration finalize / loop-control kernels.
+// centroid update V.X, and the per-iteration finalize kernel (whose last block
+// takes the loop decision).
 //
 // Reference counterparts (HicrestLaboratory/Matrix-Centric-K-Means):
 //   distance + argmin     comparisons/CPU_Kmeans/src/kmeans.cpp:86-122;
