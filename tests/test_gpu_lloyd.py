@@ -178,6 +178,22 @@ def test_determinism_and_repeat_fit(km, gpu):
     assert a[2].objective == b[2].objective and a[2].converged_iter == b[2].converged_iter
 
 
+def test_profile_between_fits(km, gpu):
+    """The per-stage timer runs iterations on the handle's state; a fit after
+    it starts again from the seeded initialisation and matches the first fit
+    (the device-side loop state, including the finalize ticket, is reset)."""
+    X, _ = helpers.synth_blobs_np(30000, 16, 20, -5, 5, 1.0, 7)
+    m = km.Lloyd(30000, 16, 20, tol=1e-4, seed=2, maxiter=30, precision="bf16x3").set_data(X)
+    a = m.fit()
+    st = m.profile(3)
+    b = m.fit()
+    m.close()
+    assert len(st) == 5 and all(v > 0 for v in st)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1].view(np.uint32), b[1].view(np.uint32))
+    assert a[2].objective == b[2].objective and a[2].iterations == b[2].iterations
+
+
 def test_device_input_and_nonfinite_rejection(km, gpu):
     import torch
     X, _ = helpers.synth_blobs_np(5000, 8, 4, -3, 3, 1.0, 2)
