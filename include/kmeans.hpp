@@ -68,20 +68,23 @@ class Kmeans {
   enum class InitMethod { random, plus_plus };
   enum class Kernel { linear, polynomial, sigmoid, gaussian };
   // Extension: arithmetic of the distance stage (linear) or of the K build.
-  enum class Precision { fp32, bf16, bf16x3 };
+  // automatic: split-BF16x3 tensor cores with exact re-scoring for the linear
+  // kernel (labels identical to fp32, several times faster), fp32 for the K
+  // build of the other kernels (K then matches an FP32 build).
+  enum class Precision { fp32, bf16, bf16x3, automatic };
 
   using KernelParams = KmeansKernelParams;
 
   Kmeans(size_t n, uint32_t d, uint32_t k, float tol, const int* seed, Point<float>** points,
          cudaDeviceProp* deviceProps, InitMethod initMethod = InitMethod::random,
-         Kernel kernel = Kernel::linear, int level = 3, Precision precision = Precision::fp32,
+         Kernel kernel = Kernel::linear, int level = 3, Precision precision = Precision::automatic,
          KernelParams kparams = KernelParams());
 
   // Extension: points given as one row-major n*d array; run() writes the
   // labels to labels_out (n entries) instead of Point objects.
   Kmeans(size_t n, uint32_t d, uint32_t k, float tol, const int* seed, const float* X,
          uint32_t* labels_out, InitMethod initMethod = InitMethod::random,
-         Kernel kernel = Kernel::linear, int level = 3, Precision precision = Precision::fp32,
+         Kernel kernel = Kernel::linear, int level = 3, Precision precision = Precision::automatic,
          KernelParams kparams = KernelParams());
 
   ~Kmeans();

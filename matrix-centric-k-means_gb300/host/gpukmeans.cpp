@@ -7,7 +7,7 @@
 //   -o/--out-file (default None)  -i/--in-file (.csv or .svm; else seeded random data)
 //   -r/--runs (default 1)  -s/--seed (default std::rand())  -t/--tolerance (default FLT_EPSILON)
 //   -c/--check 0|1 (default 0)  -h/--help
-// Extensions: -f gaussian with --sigma S; -p/--precision fp32|bf16|bf16x3;
+// Extensions: -f gaussian with --sigma S; -p/--precision auto|fp32|bf16|bf16x3;
 //   --csv-columns reference|plain (plain keeps column 0); --profile prints the
 //   per-stage [PERFORMANCE] lines of the linear path after each run.
 //
@@ -65,7 +65,7 @@ const Opt OPTS[] = {
     {'b', "init", "Method to use to initialize centroids", true},
     {'f', "kernel", "kernel function", true},
     {'l', "level", "Optimization level", true},
-    {'p', "precision", "fp32 | bf16 | bf16x3 (extension)", true},
+    {'p', "precision", "auto | fp32 | bf16 | bf16x3 (extension; auto: bf16x3 for -f linear, fp32 otherwise)", true},
     {0, "sigma", "Gaussian kernel width (extension)", true},
     {0, "csv-columns", "reference | plain (extension)", true},
     {0, "profile", "print per-stage timings (extension)", false},
@@ -250,9 +250,10 @@ int main(int argc, char** argv) {
     std::printf("Invalid kernel: %s\n", kernel_str.c_str());
     return 1;
   }
-  const std::string prec_str = get_str(args, "precision", "fp32");
+  const std::string prec_str = get_str(args, "precision", "auto");
   Kmeans::Precision precision;
-  if (prec_str == "fp32") precision = Kmeans::Precision::fp32;
+  if (prec_str == "auto") precision = Kmeans::Precision::automatic;
+  else if (prec_str == "fp32") precision = Kmeans::Precision::fp32;
   else if (prec_str == "bf16") precision = Kmeans::Precision::bf16;
   else if (prec_str == "bf16x3") precision = Kmeans::Precision::bf16x3;
   else die_arg("precision");

@@ -9,10 +9,11 @@ void check(km_status s, const char* what) {
   if (s != KM_OK) throw KmeansError(s, what);
 }
 
-km_precision to_prec(Kmeans::Precision p) {
+km_precision to_prec(Kmeans::Precision p, bool linear) {
   switch (p) {
     case Kmeans::Precision::bf16: return KM_PREC_BF16;
     case Kmeans::Precision::bf16x3: return KM_PREC_BF16X3;
+    case Kmeans::Precision::automatic: return linear ? KM_PREC_BF16X3 : KM_PREC_FP32;
     default: return KM_PREC_FP32;
   }
 }
@@ -54,7 +55,7 @@ void Kmeans::setup(const float* X, const int* seed, InitMethod initMethod, Kerne
     p.seed = seed ? *seed : 0;
     p.maxiter = 1;                       // set by run()
     p.init = initMethod == InitMethod::plus_plus ? KM_INIT_PLUSPLUS : KM_INIT_ROUND_ROBIN;
-    p.precision = to_prec(precision);
+    p.precision = to_prec(precision, kernel == Kernel::linear);
     p.conv = KM_CONV_NONE;
     p.device = 0;
     p.stream = nullptr;
@@ -80,7 +81,7 @@ void Kmeans::setup(const float* X, const int* seed, InitMethod initMethod, Kerne
     p.coef = kp.coef;
     p.sigma = kp.sigma;
     p.degree = kp.degree;
-    p.precision = to_prec(precision);
+    p.precision = to_prec(precision, kernel == Kernel::linear);
     p.k_bf16 = 0;
     p.check_converged = 0;
     p.device = 0;

@@ -71,7 +71,7 @@ def oracle_popcorn(X, kind, k, maxiter, tol, check):
     return int(it), lab, sc.value
 
 
-@pytest.mark.parametrize("prec", ["fp32", "bf16", "bf16x3"])
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "bf16x3", "auto"])
 def test_cli_linear_matches_reference_gpu_semantics(tmp_path, gpu, prec):
     X = helpers.config1_data()
     n, d = X.shape
