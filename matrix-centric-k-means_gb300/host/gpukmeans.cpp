@@ -222,6 +222,15 @@ int main(int argc, char** argv) {
     input.reset(new InputParser<float>(seed, static_cast<int>(d), n));
   }
 
+  // extension argument: validated with the others, before the device check
+  const std::string prec_str = get_str(args, "precision", "auto");
+  Kmeans::Precision precision;
+  if (prec_str == "auto") precision = Kmeans::Precision::automatic;
+  else if (prec_str == "fp32") precision = Kmeans::Precision::fp32;
+  else if (prec_str == "bf16") precision = Kmeans::Precision::bf16;
+  else if (prec_str == "bf16x3") precision = Kmeans::Precision::bf16x3;
+  else die_arg("precision");
+
   if (km_device_count() == 0) {
     std::cerr << "There are no available device(s) that support CUDA" << std::endl;
     return EXIT_CUDA_DEV;
@@ -250,13 +259,6 @@ int main(int argc, char** argv) {
     std::printf("Invalid kernel: %s\n", kernel_str.c_str());
     return 1;
   }
-  const std::string prec_str = get_str(args, "precision", "auto");
-  Kmeans::Precision precision;
-  if (prec_str == "auto") precision = Kmeans::Precision::automatic;
-  else if (prec_str == "fp32") precision = Kmeans::Precision::fp32;
-  else if (prec_str == "bf16") precision = Kmeans::Precision::bf16;
-  else if (prec_str == "bf16x3") precision = Kmeans::Precision::bf16x3;
-  else die_arg("precision");
   Kmeans::KernelParams kp;
   kp.sigma = get_float(args, "sigma", 1.0f);
   const bool profile = args.count("profile") != 0;

@@ -163,6 +163,16 @@ def test_cli_bad_values_and_unknown_option():
     assert run_cli(*args).returncode == 1
 
 
+def test_cli_precision_values():
+    """-p takes auto (the default), fp32, bf16 or bf16x3; anything else is an
+    argument error (exit 1) before the device is touched."""
+    r = run_cli(*BASE, "-p", "fp16")
+    assert r.returncode == 1 and "Invalid or missing argument" in r.stderr
+    if helpers.km().device_count() == 0:
+        for prec in ("auto", "fp32", "bf16", "bf16x3"):
+            assert run_cli(*BASE, "-p", prec).returncode == 2        # parsed; no device here
+
+
 def test_cli_invalid_input_file(tmp_path):
     r = run_cli(*BASE, "-i", tmp_path / "missing.csv")
     assert r.returncode == 4 and "Invalid input file" in r.stderr
