@@ -555,6 +555,75 @@ def kkm_arm(args):
     }
 
 
+KKM_PANEL = dict(n=262_144, d=512, k=64, lo=-1.0, hi=1.0, sigma=0.25, seed=3100, panel=8192)
+
+
+def kkm_panel_arm(args):
+    """Kernel k-means where the kernel matrix does not fit the device: n =
+    262,144, d = 512, k = 64, 64 seeded blobs (centers U[-1,1]^512, sigma
+    0.25), polynomial (x.y/d + 1)^2.  The FP32 K would be 275 GB (the
+    reference's n*n buffer, src/kmeans.cu:143); here every iteration rebuilds
+    K in panels of 8192 rows (8 GiB, split-BF16x3 on the tensor cores) and
+    streams each panel into E = K V^T."""
+    import torch
+    import helpers
+    km = helpers.km()
+    c = KKM_PANEL
+    n, d, k = c["n"], c["d"], c["k"]
+    X = km.synth_blobs(n, d, k, c["lo"], c["hi"], c["sigma"], c["seed"], nthreads=os.cpu_count() or 8)
+    Xd = torch.from_numpy(X).cuda()
+    hbm, bf16, src = peaks()
+    params = dict(gamma=1.0 / d, coef=1.0, degree=2)
+    m = km.KernelKMeans(n, d, k, kernel="polynomial", maxiter=args.warmup, precision="bf16x3", k_bf16=False,
+                        panel_rows=c["panel"], **params).set_data(Xd)
+    m.fit()                                                  # warm-up iterations
+    km.check(km.lib().km_kkm_configure(m.h, args.steps, m.p.tol, 0), "km_kkm_configure")
+    clk = Clocks(0)
+    with clk:
+        lab, r = m.fit()
+    rows = m.panel_rows()
+    m.close()
+    torch.cuda.empty_cache()
+    it_ms = r.fit_ms / r.iterations
+    mma_flops = 3 * 2.0 * n * n * d                           # split-BF16x3: three BF16 products per K entry
+    panel_bytes = 2 * n * n * 4                               # every panel written once and read once
+    pj = ROOT / "MEASURED_PEAKS.json"
+    bf16_sus = (json.loads(pj.read_text()).get("bf16_tflops_sustained") if pj.exists() else None) or 1700.0
+    # e2e through the public API from host memory: set_data (H2D of X) + fit + labels D2H
+    Xp = torch.from_numpy(X).pin_memory()
+    m = km.KernelKMeans(n, d, k, kernel="polynomial", maxiter=args.steps, precision="bf16x3", k_bf16=False,
+                        panel_rows=c["panel"], **params)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m.set_data(Xp.numpy())
+    _, r2 = m.fit()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    m.close()
+    torch.cuda.empty_cache()
+    return {
+        "metric": "iters/s (kernel k-means n=262144,d=512,k=64, K rebuilt per iteration in panels)",
+        "value": r.iterations / (r.fit_ms / 1e3), "unit": "iters/s", "n_gpus": 1, "steps": r.iterations,
+        "warmup": args.warmup, "ms_per_step": it_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "kernel k-means n=262144 d=512 k=64, polynomial (x.y/d+1)^2, FP32 K in panels "
+                               f"of {rows} rows (resident K would be 275 GB)",
+                   "n": n, "d": d, "k": k, "panel_rows": rows, "l2": "panels (8 GiB) larger than L2",
+                   "parallelism": "single GPU"},
+        "roofline": {"bound": "tensor", "achieved": mma_flops / (it_ms / 1e3) / 1e12, "peak": bf16_sus,
+                     "unit": "TFLOP/s", "frac": mma_flops / (it_ms / 1e3) / 1e12 / bf16_sus,
+                     "kernel": "whole iteration: kmat_tc_kernel panel builds (BF16 MMA flops, 3 per K entry) "
+                               "then kkm_vk_kernel panel streams, in sequence",
+                     "peak_source": src + " (bf16 sustained)", "traffic": None,
+                     "panel_hbm_gbs": panel_bytes / (it_ms / 1e3) / 1e9},
+        "clocks": clk.summary(), "gpu_launches": r.kernel_launches,
+        "e2e": {"value": r2.iterations / wall, "unit": "iters/s", "h2d_bytes_per_step": n * d * 4,
+                "d2h_bytes_per_step": n * 4,
+                "step": f"one fit from host memory: set_data (H2D of X) + {r2.iterations} iterations + labels "
+                        f"D2H; wall clock {wall * 1e3:.1f} ms"},
+    }
+
+
 def batch_arm(args):
     """512 independent Lloyd problems, n log-uniform in [1024, 65536], d in
     {2, 8, 16, 32, 64, 128, 256}, k uniform in [2, 128] (k < n), one seeded
@@ -653,10 +722,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16x3", choices=["bf16", "bf16x3", "fp32"])
-    ap.add_argument("--workload", default="lloyd", choices=["lloyd", "bigk", "kkm", "batch"],
+    ap.add_argument("--workload", default="lloyd", choices=["lloyd", "bigk", "kkm", "kkm-panel", "batch"],
                     help="lloyd: the headline n=1M d=128 k=256 workload (default); bigk: n=4M d=256 "
-                         "k=4096 BF16 points; kkm: kernel k-means n=65536 d=512 k=64; batch: 512 "
-                         "uneven problems x 8 restarts in one launch")
+                         "k=4096 BF16 points; kkm: kernel k-means n=65536 d=512 k=64; kkm-panel: kernel "
+                         "k-means n=262144 d=512 k=64 with K rebuilt in panels; batch: 512 uneven "
+                         "problems x 8 restarts in one launch")
     ap.add_argument("--stages-only", action="store_true",
                     help="lloyd only: a 5-iteration fit and the per-stage timer (Lloyd.profile) of "
                          "--precision, printed as one JSON line (a short command for profilers)")
@@ -664,7 +734,8 @@ def main():
                     help="bigk only: fewer rows than the workload's n (a smaller case for profilers)")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = 200 if (args.workload == "lloyd" and args.impl == "ours") else 20
+        args.steps = (200 if (args.workload == "lloyd" and args.impl == "ours")
+                      else 5 if args.workload == "kkm-panel" else 20)
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -678,7 +749,8 @@ def main():
         return
     if args.workload != "lloyd":
         if rank == 0:
-            line = {"bigk": bigk_arm, "kkm": kkm_arm, "batch": batch_arm}[args.workload](args)
+            line = {"bigk": bigk_arm, "kkm": kkm_arm, "kkm-panel": kkm_panel_arm,
+                    "batch": batch_arm}[args.workload](args)
             print(json.dumps(line), flush=True)
         return
     if world > 1:

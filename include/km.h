@@ -257,13 +257,27 @@ typedef struct km_kkm_params {
   int32_t check_converged; /* reference -c: stop on |score - last| < tol */
   int32_t device;
   void* stream;
+  /* Where K lives.  0: the whole n*n matrix stays resident (the reference's
+   * B, src/kmeans.cu:143), built once by km_kkm_set_data.  r > 0: only a
+   * panel of min(r, n) rows is held; every iteration rebuilds K panel by
+   * panel and streams each panel into E = K V^T, so memory is r*n instead
+   * of n*n and n is no longer capped by n^2 bytes.  The panels hold the same
+   * values as the resident matrix, so labels and score are identical.
+   * KM_KKM_PANEL_AUTO: resident when n*n fits in 90% of the free device
+   * memory, else panels sized to half of it. */
+  uint64_t panel_rows;
 } km_kkm_params;
+
+#define KM_KKM_PANEL_AUTO UINT64_MAX
 
 km_status km_kkm_create(const km_kkm_params* p, km_kkm** out);
 /* Builds K from n*d points (host or device). */
 km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device);
-/* Device time of the kernel-matrix build done by the last km_kkm_set_data. */
+/* Device time of the kernel-matrix build done by the last km_kkm_set_data
+ * (with panels: only the operand preparation, K is built per iteration). */
 km_status km_kkm_build_ms(km_kkm* h, double* ms);
+/* Rows of K per panel chosen at create (0: K resident). */
+km_status km_kkm_panel_rows(km_kkm* h, uint64_t* rows);
 /* Changes maxiter, tol and the -c stop rule before the next fit. */
 km_status km_kkm_configure(km_kkm* h, uint64_t maxiter, float tol, int32_t check_converged);
 /* init_labels: n host labels, or NULL for the reference's i % k. */

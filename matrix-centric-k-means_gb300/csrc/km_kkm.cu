@@ -98,16 +98,20 @@ __device__ __forceinline__ void kstore(void* K, uint64_t idx, float v) {
 
 // ---------------------------------------------------------------------------
 // (a) SIMT FP32 kernel-matrix GEMM: 128 x 128 tiles, 256 threads, 8 x 8
-// micro-tiles, K chunks of 16 through shared memory.
+// micro-tiles, K chunks of 16 through shared memory.  Builds rows
+// [row0, row_end) of K into K (row stride n, first row = row0); with `stop`
+// set it does nothing once the fit has stopped (panels rebuilt per iteration).
 // ---------------------------------------------------------------------------
 template <bool OUT_BF16>
 __global__ void __launch_bounds__(256)
 kmat_f32_kernel(const float* __restrict__ X, const float* __restrict__ xn2, uint64_t n, uint32_t d,
-                KFn f, void* __restrict__ K, float* __restrict__ diag) {
+                uint64_t row0, uint64_t row_end, KFn f, void* __restrict__ K, float* __restrict__ diag,
+                const DevState* stop) {
+  if (stop && stop->done) return;
   __shared__ __align__(16) float As[16][128 + 4];
   __shared__ __align__(16) float Bs[16][128 + 4];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const uint64_t m0 = (uint64_t)blockIdx.y * 128, c0 = (uint64_t)blockIdx.x * 128;
+  const uint64_t m0 = row0 + (uint64_t)blockIdx.y * 128, c0 = (uint64_t)blockIdx.x * 128;
   float acc[8][8];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
@@ -119,7 +123,7 @@ kmat_f32_kernel(const float* __restrict__ X, const float* __restrict__ xn2, uint
       const int idx = e * 256 + tid;
       const int r = idx >> 4, kk = idx & 15;
       const uint32_t col = kc + kk;
-      As[kk][r] = (m0 + r < n && col < d) ? X[(m0 + r) * d + col] : 0.0f;
+      As[kk][r] = (m0 + r < row_end && col < d) ? X[(m0 + r) * d + col] : 0.0f;
       Bs[kk][r] = (c0 + r < n && col < d) ? X[(c0 + r) * d + col] : 0.0f;
     }
     __syncthreads();
@@ -138,14 +142,14 @@ kmat_f32_kernel(const float* __restrict__ X, const float* __restrict__ xn2, uint
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const uint64_t row = m0 + ty * 8 + i;
-    if (row >= n) continue;
+    if (row >= row_end) continue;
     const float ni = xn2[row];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const uint64_t col = c0 + tx * 8 + j;
       if (col >= n) continue;
       const float v = kfn_apply(f, acc[i][j], ni, xn2[col]);
-      kstore<OUT_BF16>(K, row * n + col, v);
+      kstore<OUT_BF16>(K, (row - row0) * n + col, v);
       if (diag && row == col) diag[row] = v;
     }
   }
@@ -159,7 +163,9 @@ kmat_f32_kernel(const float* __restrict__ X, const float* __restrict__ xn2, uint
 // columns); eight epilogue warps (two sets, one per buffer; warp w on TMEM
 // lanes 32*(w%4)) read the accumulator 64 columns at a time, apply f and store
 // K.  Every wait is bounded (2 s) and a timeout raises KM_DEVERR_TIMEOUT after
-// draining this CTA's copies and MMAs.
+// draining this CTA's copies and MMAs.  The kernel builds rows
+// [prow0, prow_end) of K into K (row stride n, first row = prow0): all of K,
+// or one panel of it; with skip_done it does nothing once the fit has stopped.
 // ---------------------------------------------------------------------------
 namespace {
 constexpr int KM_M = 128, KM_N = 256;
@@ -193,8 +199,10 @@ template <bool X3, bool OUT_BF16, int KIND>
 __global__ void __launch_bounds__(384, 1)
 kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tAlo,
                const __grid_constant__ CUtensorMap tB, const __grid_constant__ CUtensorMap tBlo,
-               const float* __restrict__ xn2, uint64_t n, uint32_t KB, uint32_t S, KFn f,
-               void* __restrict__ K, float* __restrict__ diag, int vec, DevState* st) {
+               const float* __restrict__ xn2, uint64_t n, uint64_t prow0, uint64_t prow_end, uint32_t KB,
+               uint32_t S, KFn f, void* __restrict__ K, float* __restrict__ diag, int vec, int skip_done,
+               DevState* st) {
+  if (skip_done && st->done) return;   // uniform over the grid: written by an earlier launch
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
@@ -202,7 +210,7 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
   float* stg_all = reinterpret_cast<float*>(smem + (size_t)S * stage_bytes);    // [8 warps][32][32]
   KmSmem* ts = reinterpret_cast<KmSmem*>(smem + (size_t)S * stage_bytes + KM_STG_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint64_t mt = (n + KM_M - 1) / KM_M, nt = (n + KM_N - 1) / KM_N;
+  const uint64_t mt = (prow_end - prow0 + KM_M - 1) / KM_M, nt = (n + KM_N - 1) / KM_N;
   const uint64_t ntiles = mt * nt;
   if (threadIdx.x == 0) {
     for (uint32_t s = 0; s < S; ++s) { mbar_init(&ts->full[s], 1); mbar_init(&ts->empty[s], 1); }
@@ -235,10 +243,10 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
           if (!mbar_wait_bounded(&ts->empty[s], ph ^ 1u, abort_flag, KWAIT_NS)) { fail(1); ok = false; break; }
           mbar_arrive_expect_tx(&ts->full[s], stage_bytes);
           uint8_t* dst = smem + (size_t)s * stage_bytes;
-          tma_load_2d(dst, &tA, (int)(kb * 64), (int)(mi * KM_M), &ts->full[s]);
+          tma_load_2d(dst, &tA, (int)(kb * 64), (int)(prow0 + mi * KM_M), &ts->full[s]);
           tma_load_2d(dst + KA_BYTES, &tB, (int)(kb * 64), (int)(nj * KM_N), &ts->full[s]);
           if (X3) {
-            tma_load_2d(dst + KA_BYTES + KB_BYTES, &tAlo, (int)(kb * 64), (int)(mi * KM_M), &ts->full[s]);
+            tma_load_2d(dst + KA_BYTES + KB_BYTES, &tAlo, (int)(kb * 64), (int)(prow0 + mi * KM_M), &ts->full[s]);
             tma_load_2d(dst + 2 * KA_BYTES + KB_BYTES, &tBlo, (int)(kb * 64), (int)(nj * KM_N), &ts->full[s]);
           }
         }
@@ -296,9 +304,9 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
     for (uint64_t tile = blockIdx.x + (uint64_t)set * gridDim.x; tile < ntiles;
          tile += 2ull * gridDim.x, t += 2) {
       uint64_t mi, nj;
-        kmat_tile(tile, mt, nt, mi, nj);
-      const uint64_t row = mi * KM_M + r, c0 = nj * KM_N;
-      const float ni = (row < n) ? xn2[row] : 0.0f;
+      kmat_tile(tile, mt, nt, mi, nj);
+      const uint64_t row = prow0 + mi * KM_M + r, c0 = nj * KM_N;
+      const float ni = (row < prow_end) ? xn2[row] : 0.0f;
       // column norms only matter for the Gaussian kernel (broadcast loads)
       auto colnorm = [&](uint64_t c) -> float {
         return (KIND == KM_KERNEL_GAUSSIAN && c < n) ? __ldg(xn2 + c) : 0.0f;
@@ -310,7 +318,7 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
       // columns, 16-byte chunks XOR-swizzled by row) and leave as whole
       // 128-byte row segments: eight lanes per row, four rows per store.
       float* stg = stg_all + (size_t)(warp - 4) * 32 * 32;
-      const uint64_t row0 = mi * KM_M + (uint64_t)q * 32u;          // first row of this warp
+      const uint64_t row0 = prow0 + mi * KM_M + (uint64_t)q * 32u;  // first row of this warp
       for (uint32_t pr = 0; pr < KM_N / 64; ++pr) {
         uint32_t acc[64];
         tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
@@ -326,7 +334,7 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
             o.y = kfn_apply_k<KIND>(f, __uint_as_float(acc[h * 32 + 4 * c + 1]), ni, colnorm(cb + 4 * c + 1));
             o.z = kfn_apply_k<KIND>(f, __uint_as_float(acc[h * 32 + 4 * c + 2]), ni, colnorm(cb + 4 * c + 2));
             o.w = kfn_apply_k<KIND>(f, __uint_as_float(acc[h * 32 + 4 * c + 3]), ni, colnorm(cb + 4 * c + 3));
-            if (diag && row < n) {
+            if (diag && row < prow_end) {
               if (cb + 4 * c + 0 == row) diag[row] = o.x;
               if (cb + 4 * c + 1 == row) diag[row] = o.y;
               if (cb + 4 * c + 2 == row) diag[row] = o.z;
@@ -341,9 +349,9 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
             const uint32_t ch = (uint32_t)lane & 7u;                           // 16-byte chunk of the row
             const float4 o = *reinterpret_cast<const float4*>(stg + rr * 32 + ((ch ^ (rr & 7u)) * 4u));
             const uint64_t grow = row0 + rr, gcol = cb + ch * 4u;
-            if (grow >= n) continue;
+            if (grow >= prow_end) continue;
             if (OUT_BF16) {
-              __nv_bfloat16* Kp = reinterpret_cast<__nv_bfloat16*>(K) + grow * n + gcol;
+              __nv_bfloat16* Kp = reinterpret_cast<__nv_bfloat16*>(K) + (grow - prow0) * n + gcol;
               if (vec && gcol + 3 < n) {
                 const __nv_bfloat162 a = __floats2bfloat162_rn(o.x, o.y), b = __floats2bfloat162_rn(o.z, o.w);
                 uint2 u;
@@ -357,7 +365,7 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
                 if (gcol + 3 < n) Kp[3] = __float2bfloat16_rn(o.w);
               }
             } else {
-              float* Kp = reinterpret_cast<float*>(K) + grow * n + gcol;
+              float* Kp = reinterpret_cast<float*>(K) + (grow - prow0) * n + gcol;
               if (vec && gcol + 3 < n) {
                 *reinterpret_cast<float4*>(Kp) = o;
               } else {
@@ -383,34 +391,45 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
 
 // ---------------------------------------------------------------------------
 // (c) E = K V^T.  One warp per row of K at a time; the labels of all n points
-// sit in shared memory as bytes (k <= 256); every lane accumulates its columns
-// into private bins bins[c][lane] (no atomics, fixed order), then each lane
-// reduces two bins over the 32 lanes in lane order.  K rows are read once with
-// 16-byte (FP32) or 8-byte (BF16) loads.
+// are bytes (k <= 256), in shared memory when they fit next to the bins
+// (GLAB false) or else read from a global byte copy (GLAB true, L2-resident);
+// every lane accumulates its columns into private bins bins[c][lane] (no
+// atomics, fixed order), then each lane reduces two bins over the 32 lanes in
+// lane order.  K rows are read once with 16-byte (FP32) or 8-byte (BF16)
+// loads.  Rows [row0, row_end) are done; K holds them from row row0 on (the
+// whole matrix with row0 = 0, or one panel).  Both label sources give the
+// same sums in the same order.
 // ---------------------------------------------------------------------------
-template <bool KBF16>
+template <bool KBF16, bool GLAB>
 __global__ void __launch_bounds__(512)
 kkm_vk_kernel(const void* __restrict__ K, uint64_t n, uint32_t k, const uint32_t* __restrict__ labels,
-              float* __restrict__ E, DevState* st) {
+              const uint8_t* __restrict__ lab8, uint64_t row0, uint64_t row_end, float* __restrict__ E,
+              DevState* st) {
   if (st->done) return;
   extern __shared__ __align__(16) uint8_t kk_smem[];
-  uint8_t* lab = kk_smem;                                            // n bytes
-  float* bins = reinterpret_cast<float*>(kk_smem + ((n + 15) & ~15ull));  // [warps][k][32]
-  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) lab[i] = (uint8_t)labels[i];
-  __syncthreads();
+  const uint8_t* lab = GLAB ? lab8 : kk_smem;                        // n bytes
+  float* bins = reinterpret_cast<float*>(kk_smem + (GLAB ? 0ull : ((n + 15) & ~15ull)));  // [warps][k][32]
+  if (!GLAB) {
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) kk_smem[i] = (uint8_t)labels[i];
+    __syncthreads();
+  }
+  auto lab4 = [&](uint64_t j) -> uint32_t {     // labels j..j+3 (j % 4 == 0)
+    return GLAB ? __ldg(reinterpret_cast<const uint32_t*>(lab + j)) : *reinterpret_cast<const uint32_t*>(lab + j);
+  };
+  auto lab1 = [&](uint64_t j) -> uint32_t { return GLAB ? (uint32_t)__ldg(lab + j) : (uint32_t)lab[j]; };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float* B = bins + (size_t)warp * k * 32;
   for (uint32_t c = 0; c < k; ++c) B[c * 32 + lane] = 0.0f;
   __syncwarp();
   const uint32_t wpb = blockDim.x >> 5;
   const uint64_t nw = (uint64_t)gridDim.x * wpb;
-  for (uint64_t row = (uint64_t)blockIdx.x * wpb + warp; row < n; row += nw) {
+  for (uint64_t row = row0 + (uint64_t)blockIdx.x * wpb + warp; row < row_end; row += nw) {
     // With n % 4 == 0 every row starts 16-byte (FP32) / 8-byte (BF16)
     // aligned: lane l takes columns 4l..4l+3 of each 128-column stride.
     // Otherwise one column per lane with plain loads.
     const bool v4 = (n & 3) == 0;
     if (KBF16) {
-      const __nv_bfloat16* Kr = reinterpret_cast<const __nv_bfloat16*>(K) + row * n;
+      const __nv_bfloat16* Kr = reinterpret_cast<const __nv_bfloat16*>(K) + (row - row0) * n;
       if (v4) {
         // U loads in flight per lane before the (ordered) bin updates
         constexpr int U = 16;
@@ -421,7 +440,7 @@ kkm_vk_kernel(const void* __restrict__ K, uint64_t n, uint32_t k, const uint32_t
           for (int u = 0; u < U; ++u) {
             const uint64_t j = j0 + 128ull * u;
             raw[u] = j < n ? __ldg(reinterpret_cast<const uint2*>(Kr + j)) : make_uint2(0u, 0u);
-            l4[u] = j < n ? *reinterpret_cast<const uint32_t*>(lab + j) : 0u;
+            l4[u] = j < n ? lab4(j) : 0u;
           }
 #pragma unroll
           for (int u = 0; u < U; ++u) {
@@ -435,10 +454,10 @@ kkm_vk_kernel(const void* __restrict__ K, uint64_t n, uint32_t k, const uint32_t
           }
         }
       } else {
-        for (uint64_t j = lane; j < n; j += 32) B[lab[j] * 32 + lane] += __bfloat162float(Kr[j]);
+        for (uint64_t j = lane; j < n; j += 32) B[lab1(j) * 32 + lane] += __bfloat162float(Kr[j]);
       }
     } else {
-      const float* Kr = reinterpret_cast<const float*>(K) + row * n;
+      const float* Kr = reinterpret_cast<const float*>(K) + (row - row0) * n;
       if (v4) {
         // U loads in flight per lane before the (ordered) bin updates
         constexpr int U = 8;
@@ -449,7 +468,7 @@ kkm_vk_kernel(const void* __restrict__ K, uint64_t n, uint32_t k, const uint32_t
           for (int u = 0; u < U; ++u) {
             const uint64_t j = j0 + 128ull * u;
             v[u] = j < n ? __ldg(reinterpret_cast<const float4*>(Kr + j)) : make_float4(0.f, 0.f, 0.f, 0.f);
-            l4[u] = j < n ? *reinterpret_cast<const uint32_t*>(lab + j) : 0u;
+            l4[u] = j < n ? lab4(j) : 0u;
           }
 #pragma unroll
           for (int u = 0; u < U; ++u) {
@@ -461,7 +480,7 @@ kkm_vk_kernel(const void* __restrict__ K, uint64_t n, uint32_t k, const uint32_t
           }
         }
       } else {
-        for (uint64_t j = lane; j < n; j += 32) B[lab[j] * 32 + lane] += Kr[j];
+        for (uint64_t j = lane; j < n; j += 32) B[lab1(j) * 32 + lane] += Kr[j];
       }
     }
     __syncwarp();
@@ -555,14 +574,24 @@ __global__ void kkm_control_kernel(const double* __restrict__ part, int np, Loop
   }
 }
 
+// dst8 (optional): the byte copy of the labels that the V.K kernel reads when
+// they do not fit shared memory.
 __global__ void kkm_copy_labels_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
-                                       uint64_t n, DevState* st) {
+                                       uint8_t* __restrict__ dst8, uint64_t n, DevState* st) {
   // runs after the control kernel: the labels of the final iteration are
   // copied too (the done flag is set by then), so only stop after copying.
   if (st->iter == 0) return;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x)
+       i += (uint64_t)gridDim.x * blockDim.x) {
     dst[i] = src[i];
+    if (dst8) dst8[i] = (uint8_t)src[i];
+  }
+}
+
+__global__ void kkm_label_bytes_kernel(const uint32_t* __restrict__ src, uint8_t* __restrict__ dst8, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    dst8[i] = (uint8_t)src[i];
 }
 
 }  // namespace km
@@ -572,8 +601,12 @@ using namespace km;
 struct km_kkm {
   km_kkm_params p;
   LloydEngine eng;          // sort machinery, stream, state (no Lloyd buffers used)
-  void* K = nullptr;        // n x n, float or bf16
+  void* K = nullptr;        // n x n (resident) or panel x n (panels), float or bf16
   float* diag = nullptr;
+  uint64_t panel = 0;       // rows of K per panel, 0 when K is resident
+  uint8_t* lab8 = nullptr;  // byte labels for the V.K kernel when they do not fit shared memory
+  bool glab = false;
+  uint64_t kpi = 0;         // kernels launched per iteration
   float* E = nullptr;       // n x k
   double* ct = nullptr;
   uint32_t* lab = nullptr;  // current labels
@@ -608,26 +641,38 @@ km_status kfn_valid(int kind, int degree, float sigma) {
   return KM_OK;
 }
 
-// Builds K (and diag) from points X (device, n x d) on stream s.  For the
-// tensor-core precisions it uses BF16 copies prepared by the engine.
+// Gaussian kernel on the tensor cores: norms of the BF16 operands (see
+// kmat_operand_norms_kernel); they overwrite xn2, which the kernel-matrix path
+// does not otherwise use.  Once per set of points.
+km_status prepare_kmat_norms(LloydEngine& e, uint64_t n, const KFn& f, int precision) {
+  if (precision == KM_PREC_FP32 || f.kind != KM_KERNEL_GAUSSIAN) return KM_OK;
+  kmat_operand_norms_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, e.stream>>>(
+      e.Xb, precision == KM_PREC_BF16X3 ? e.Xlo : nullptr, n, e.dp, e.xn2);
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
+
+// Builds rows [row0, row_end) of K (and of diag) from points X (device,
+// n x d) on the engine's stream into K (row stride n, first row = row0).  For
+// the tensor-core precisions it uses the BF16 copies prepared by the engine
+// and the operand norms of prepare_kmat_norms.  skip_done: the launch does
+// nothing once the fit has stopped (panels rebuilt inside the iteration).
 km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32_t d, const KFn& f,
-                              int precision, bool out_bf16, void* K, float* diag) {
+                              int precision, bool out_bf16, void* K, float* diag, uint64_t row0,
+                              uint64_t row_end, bool skip_done) {
   cudaStream_t s = e.stream;
+  if (row0 >= row_end || row_end > n) return KM_ERR_ARG;
+  const uint64_t rows = row_end - row0;
   if (precision == KM_PREC_FP32) {
-    dim3 grid((unsigned)((n + 127) / 128), (unsigned)((n + 127) / 128));
-    if (out_bf16) kmat_f32_kernel<true><<<grid, 256, 0, s>>>(X, e.xn2, n, d, f, K, diag);
-    else kmat_f32_kernel<false><<<grid, 256, 0, s>>>(X, e.xn2, n, d, f, K, diag);
+    if ((rows + 127) / 128 > 65535) return KM_ERR_UNSUPPORTED;
+    dim3 grid((unsigned)((n + 127) / 128), (unsigned)((rows + 127) / 128));
+    const DevState* stop = skip_done ? e.st : nullptr;
+    if (out_bf16) kmat_f32_kernel<true><<<grid, 256, 0, s>>>(X, e.xn2, n, d, row0, row_end, f, K, diag, stop);
+    else kmat_f32_kernel<false><<<grid, 256, 0, s>>>(X, e.xn2, n, d, row0, row_end, f, K, diag, stop);
     KM_CUDA_TRY(cudaGetLastError());
     return KM_OK;
   }
   const bool x3 = precision == KM_PREC_BF16X3;
-  // Gaussian kernel: norms of the BF16 operands (see kmat_operand_norms_kernel);
-  // they overwrite xn2, which the kernel-matrix path does not otherwise use.
-  if (f.kind == KM_KERNEL_GAUSSIAN) {
-    kmat_operand_norms_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(e.Xb, x3 ? e.Xlo : nullptr, n,
-                                                                                e.dp, e.xn2);
-    KM_CUDA_TRY(cudaGetLastError());
-  }
   CUtensorMap tA{}, tAlo{}, tB{}, tBlo{};
   KM_TRY(encode_tmap_bf16(&tA, e.Xb, e.dp, n, 64, KM_M));
   KM_TRY(encode_tmap_bf16(&tB, e.Xb, e.dp, n, 64, KM_N));
@@ -645,15 +690,16 @@ km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32
   if (S > 8) S = 8;
   if (S < 2) return KM_ERR_UNSUPPORTED;
   const size_t smem = fixed + S * stage;
-  const uint64_t tiles = ((n + KM_M - 1) / KM_M) * ((n + KM_N - 1) / KM_N);
+  const uint64_t tiles = ((rows + KM_M - 1) / KM_M) * ((n + KM_N - 1) / KM_N);
   const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)e.num_sms);
   const int vec = (n % 4 == 0) && (reinterpret_cast<uintptr_t>(K) % 16 == 0);
 #define KM_LAUNCH_KMAT(X3_, BF_, KIND_)                                                            \
   do {                                                                                             \
     KM_CUDA_TRY(cudaFuncSetAttribute(kmat_tc_kernel<X3_, BF_, KIND_>,                              \
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));     \
-    kmat_tc_kernel<X3_, BF_, KIND_><<<grid, 384, smem, s>>>(tA, tAlo, tB, tBlo, e.xn2, n, KBn,     \
-                                                            (uint32_t)S, f, K, diag, vec, e.st);   \
+    kmat_tc_kernel<X3_, BF_, KIND_><<<grid, 384, smem, s>>>(tA, tAlo, tB, tBlo, e.xn2, n, row0,    \
+                                                            row_end, KBn, (uint32_t)S, f, K, diag, \
+                                                            vec, skip_done ? 1 : 0, e.st);         \
   } while (0)
 #define KM_LAUNCH_KIND(X3_, BF_)                                                                   \
   do {                                                                                             \
@@ -672,24 +718,54 @@ km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32
   return KM_OK;
 }
 
-// V.K, 4 sort kernels, c~, distances/argmin, control, label copy
-constexpr uint64_t KKM_KERNELS_PER_ITER = 9;
+// Per iteration: V.K (with the K panel builds before each panel's V.K when
+// K is not resident), 4 sort kernels, c~, distances/argmin, control, label copy.
+uint64_t kkm_kernels_per_iter(uint64_t n, uint64_t panel) {
+  return panel ? 8 + 2 * ((n + panel - 1) / panel) : 9;
+}
+
+km_status kkm_launch_vk(km_kkm* h, uint64_t r0, uint64_t r1) {
+  LloydEngine& e = h->eng;
+  const dim3 grid(e.num_sms), block(h->vk_warps * 32);
+  const uint64_t n = h->p.n;
+  const uint32_t k = h->p.k;
+  cudaStream_t s = e.stream;
+  if (h->p.k_bf16) {
+    if (h->glab) kkm_vk_kernel<true, true><<<grid, block, h->vk_smem, s>>>(h->K, n, k, h->lab, h->lab8, r0, r1, h->E, e.st);
+    else kkm_vk_kernel<true, false><<<grid, block, h->vk_smem, s>>>(h->K, n, k, h->lab, h->lab8, r0, r1, h->E, e.st);
+  } else {
+    if (h->glab) kkm_vk_kernel<false, true><<<grid, block, h->vk_smem, s>>>(h->K, n, k, h->lab, h->lab8, r0, r1, h->E, e.st);
+    else kkm_vk_kernel<false, false><<<grid, block, h->vk_smem, s>>>(h->K, n, k, h->lab, h->lab8, r0, r1, h->E, e.st);
+  }
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
+}
 
 km_status kkm_enqueue_iteration(km_kkm* h, const LoopConsts& lc) {
   LloydEngine& e = h->eng;
   const uint64_t n = h->p.n;
   const uint32_t k = h->p.k;
   cudaStream_t s = e.stream;
-  if (h->p.k_bf16)
-    kkm_vk_kernel<true><<<e.num_sms, h->vk_warps * 32, h->vk_smem, s>>>(h->K, n, k, h->lab, h->E, e.st);
-  else
-    kkm_vk_kernel<false><<<e.num_sms, h->vk_warps * 32, h->vk_smem, s>>>(h->K, n, k, h->lab, h->E, e.st);
+  if (h->panel) {
+    // K is not resident: rebuild it panel by panel, each panel streamed into
+    // its rows of E before the next one overwrites it (stream order)
+    const KFn f = make_kfn(h->p);
+    for (uint64_t r0 = 0; r0 < n; r0 += h->panel) {
+      const uint64_t r1 = std::min<uint64_t>(n, r0 + h->panel);
+      KM_TRY(build_kernel_matrix(e, e.X, n, h->p.d, f, h->p.precision, h->p.k_bf16 != 0, h->K, nullptr, r0, r1,
+                                 true));
+      KM_TRY(kkm_launch_vk(h, r0, r1));
+    }
+  } else {
+    KM_TRY(kkm_launch_vk(h, 0, n));
+  }
   KM_TRY(e.enqueue_sort(h->lab));
   kkm_ctilde_kernel<<<(k * 32 + 255) / 256, 256, 0, s>>>(h->E, k, e.perm, e.cstart, h->ct, e.st);
   kkm_dist_kernel<<<h->dist_blocks, 256, 2 * k * sizeof(float), s>>>(h->E, n, k, e.counts, h->ct, h->nlab,
                                                                       h->part, e.st);
   kkm_control_kernel<<<1, 32, 0, s>>>(h->part, h->dist_blocks, lc, h->p.check_converged, e.st);
-  kkm_copy_labels_kernel<<<(unsigned)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(h->nlab, h->lab, n, e.st);
+  kkm_copy_labels_kernel<<<(unsigned)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+      h->nlab, h->lab, h->glab ? h->lab8 : nullptr, n, e.st);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }
@@ -711,7 +787,9 @@ km_status km_kernel_matrix(const float* X_dev, uint64_t n, uint32_t d, int32_t k
   KM_TRY(e.set_points(X_dev, true, false));
   km_kkm_params p{};
   p.kernel_fn = kernel_fn; p.gamma = gamma; p.coef = coef; p.degree = degree; p.sigma = sigma;
-  KM_TRY(build_kernel_matrix(e, X_dev, n, d, make_kfn(p), precision, out_bf16 != 0, K_dev, diag_dev));
+  const KFn f = make_kfn(p);
+  KM_TRY(prepare_kmat_norms(e, n, f, precision));
+  KM_TRY(build_kernel_matrix(e, X_dev, n, d, f, precision, out_bf16 != 0, K_dev, diag_dev, 0, n, false));
   return e.check_device_error();
 }
 
@@ -719,40 +797,72 @@ km_status km_kkm_create(const km_kkm_params* p, km_kkm** out) {
   if (!p || !out) return KM_ERR_ARG;
   *out = nullptr;
   if (p->n == 0 || p->d == 0 || p->k == 0 || p->k > p->n || p->maxiter == 0) return KM_ERR_ARG;
-  if (p->k > 256) return KM_ERR_UNSUPPORTED;   // byte labels in shared memory
+  if (p->k > 256) return KM_ERR_UNSUPPORTED;   // byte labels
   if (!(p->tol >= 0.0f)) return KM_ERR_ARG;
   KM_TRY(kfn_valid(p->kernel_fn, p->degree, p->sigma));
   const uint64_t nn = p->n * p->n;
   if (nn / p->n != p->n) return KM_ERR_ARG;
-  // per-warp bins (k x 32 floats) next to the byte labels; more warps keep
-  // more K rows in flight
+  // V.K: per-warp bins (k x 32 floats), next to the byte labels when those
+  // fit beside eight warps' bins, else the labels come from a global byte
+  // copy; more warps keep more K rows in flight
+  constexpr size_t SMEM = 227 * 1024;
   const size_t lab_bytes = (p->n + 15) & ~15ull, bin_bytes = (size_t)p->k * 32 * sizeof(float);
-  if (lab_bytes + 8 * bin_bytes > 227 * 1024) return KM_ERR_UNSUPPORTED;
-  uint32_t vk_warps = 8;
-  while (vk_warps < 16 && lab_bytes + (size_t)(vk_warps + 1) * bin_bytes <= 227 * 1024) ++vk_warps;
-  const size_t vk_smem = lab_bytes + (size_t)vk_warps * bin_bytes;
+  const bool glab = lab_bytes + 8 * bin_bytes > SMEM;
+  const size_t lb = glab ? 0 : lab_bytes;
+  uint32_t vk_warps = glab ? 1 : 8;
+  while (vk_warps < 16 && lb + (size_t)(vk_warps + 1) * bin_bytes <= SMEM) ++vk_warps;
+  const size_t vk_smem = lb + (size_t)vk_warps * bin_bytes;
+  if (vk_smem > SMEM) return KM_ERR_UNSUPPORTED;
   km_kkm* h = new (std::nothrow) km_kkm();
   if (!h) return KM_ERR_ALLOC;
   h->p = *p;
   h->vk_smem = vk_smem;
   h->vk_warps = vk_warps;
+  h->glab = glab;
   km_status s = h->eng.init(p->n, p->d, p->k, p->precision, p->device, p->stream, true);
   auto fail = [&](km_status st) { km_kkm_destroy(h); return st; };
   if (s != KM_OK) return fail(s);
-  const size_t kbytes = nn * (p->k_bf16 ? 2 : 4);
-  if (cudaMalloc(&h->K, kbytes) != cudaSuccess || cudaMalloc(&h->diag, sizeof(float) * p->n) != cudaSuccess ||
+  if (cudaMalloc(&h->diag, sizeof(float) * p->n) != cudaSuccess ||
       cudaMalloc(&h->E, sizeof(float) * p->n * p->k) != cudaSuccess ||
       cudaMalloc(&h->ct, sizeof(double) * p->k) != cudaSuccess ||
       cudaMalloc(&h->lab, sizeof(uint32_t) * p->n) != cudaSuccess ||
       cudaMalloc(&h->nlab, sizeof(uint32_t) * p->n) != cudaSuccess ||
-      cudaMalloc(&h->part, sizeof(double) * 1024) != cudaSuccess) {
+      cudaMalloc(&h->part, sizeof(double) * 1024) != cudaSuccess ||
+      (glab && cudaMalloc(&h->lab8, lab_bytes) != cudaSuccess)) {
     (void)cudaGetLastError();
     return fail(KM_ERR_ALLOC);
   }
+  // K last: resident (n x n) or one panel of rows
+  const size_t bpe = p->k_bf16 ? 2 : 4;
+  uint64_t panel = 0;
+  if (p->panel_rows == KM_KKM_PANEL_AUTO) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { (void)cudaGetLastError(); return fail(KM_ERR_CUDA); }
+    if ((double)nn * bpe > 0.9 * (double)fr) {
+      const uint64_t r = (uint64_t)(0.5 * (double)fr / ((double)p->n * bpe)) / 128 * 128;
+      panel = std::min<uint64_t>(std::max<uint64_t>(r, 128), p->n);
+    }
+  } else if (p->panel_rows > 0) {
+    panel = std::min<uint64_t>(p->panel_rows, p->n);
+  }
+  h->panel = panel;
+  h->kpi = kkm_kernels_per_iter(p->n, panel);
+  const size_t kbytes = (panel ? panel * p->n : nn) * bpe;
+  if (cudaMalloc(&h->K, kbytes) != cudaSuccess) { (void)cudaGetLastError(); return fail(KM_ERR_ALLOC); }
   h->dist_blocks = (int)std::min<uint64_t>((p->n + 255) / 256, 1024);
-  if (cudaFuncSetAttribute(kkm_vk_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vk_smem) != cudaSuccess ||
-      cudaFuncSetAttribute(kkm_vk_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vk_smem) != cudaSuccess ||
-      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess ||
+  bool attr_ok = true;
+  if (glab) {
+    attr_ok = cudaFuncSetAttribute(kkm_vk_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)vk_smem) == cudaSuccess &&
+              cudaFuncSetAttribute(kkm_vk_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)vk_smem) == cudaSuccess;
+  } else {
+    attr_ok = cudaFuncSetAttribute(kkm_vk_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)vk_smem) == cudaSuccess &&
+              cudaFuncSetAttribute(kkm_vk_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)vk_smem) == cudaSuccess;
+  }
+  if (!attr_ok || cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess ||
       cudaMallocHost(reinterpret_cast<void**>(&h->h_done), sizeof(int32_t)) != cudaSuccess) {
     (void)cudaGetLastError();
     return fail(KM_ERR_CUDA);
@@ -765,9 +875,13 @@ km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device) {
   if (!h || !X) return KM_ERR_ARG;
   LloydEngine& e = h->eng;
   KM_TRY(e.set_points(X, on_device != 0, true));
+  const KFn f = make_kfn(h->p);
   KM_CUDA_TRY(cudaEventRecord(h->ev0, e.stream));
-  KM_TRY(build_kernel_matrix(e, e.X, h->p.n, h->p.d, make_kfn(h->p), h->p.precision, h->p.k_bf16 != 0,
-                             h->K, h->diag));
+  KM_TRY(prepare_kmat_norms(e, h->p.n, f, h->p.precision));
+  // with panels, K is built inside every iteration instead
+  if (!h->panel)
+    KM_TRY(build_kernel_matrix(e, e.X, h->p.n, h->p.d, f, h->p.precision, h->p.k_bf16 != 0, h->K, h->diag, 0,
+                               h->p.n, false));
   KM_CUDA_TRY(cudaEventRecord(h->ev1, e.stream));
   KM_CUDA_TRY(cudaEventSynchronize(h->ev1));
   float ms = 0.f;
@@ -775,6 +889,12 @@ km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device) {
   h->kbuild_ms = ms;
   KM_TRY(e.check_device_error());
   h->ready = true;
+  return KM_OK;
+}
+
+km_status km_kkm_panel_rows(km_kkm* h, uint64_t* rows) {
+  if (!h || !rows) return KM_ERR_ARG;
+  *rows = h->panel;
   return KM_OK;
 }
 
@@ -808,6 +928,11 @@ km_status km_kkm_fit(km_kkm* h, const uint32_t* init_labels, uint32_t* labels_ou
     round_robin_labels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, e.stream>>>(h->lab, n, h->p.k);
     KM_CUDA_TRY(cudaGetLastError());
   }
+  if (h->glab) {
+    kkm_label_bytes_kernel<<<(unsigned)std::min<uint64_t>((n + 255) / 256, 4096), 256, 0, e.stream>>>(h->lab,
+                                                                                                   h->lab8, n);
+    KM_CUDA_TRY(cudaGetLastError());
+  }
   LoopConsts lc{h->p.maxiter, h->p.tol, h->p.check_converged ? KM_CONV_SCORE : KM_CONV_NONE, 0};
   KM_CUDA_TRY(cudaEventRecord(h->ev0, e.stream));
   uint64_t launched = 0, batch = h->p.check_converged ? 4 : h->p.maxiter;
@@ -836,7 +961,7 @@ km_status km_kkm_fit(km_kkm* h, const uint32_t* init_labels, uint32_t* labels_ou
     res->objective = s.objective;
     res->score = s.score;
     res->fit_ms = ms;
-    res->kernel_launches = launched * KKM_KERNELS_PER_ITER;
+    res->kernel_launches = launched * h->kpi;
   }
   return KM_OK;
 }
@@ -850,6 +975,7 @@ void km_kkm_destroy(km_kkm* h) {
   if (h->ct) cudaFree(h->ct);
   if (h->lab) cudaFree(h->lab);
   if (h->nlab) cudaFree(h->nlab);
+  if (h->lab8) cudaFree(h->lab8);
   if (h->part) cudaFree(h->part);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);

@@ -86,6 +86,7 @@ void Kmeans::setup(const float* X, const int* seed, InitMethod initMethod, Kerne
     p.check_converged = 0;
     p.device = 0;
     p.stream = nullptr;
+    p.panel_rows = KM_KKM_PANEL_AUTO;    // K resident when it fits, else rebuilt in panels
     check(km_kkm_create(&p, &kkm_), "km_kkm_create");
     km_status s = km_kkm_set_data(kkm_, X, 0);
     if (s != KM_OK) {

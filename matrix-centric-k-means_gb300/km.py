@@ -50,9 +50,10 @@ class KkmParams(C.Structure):
                 ("maxiter", C.c_uint64), ("kernel_fn", C.c_int32), ("gamma", C.c_float),
                 ("coef", C.c_float), ("sigma", C.c_float), ("degree", C.c_int32),
                 ("precision", C.c_int32), ("k_bf16", C.c_int32), ("check_converged", C.c_int32),
-                ("device", C.c_int32), ("stream", C.c_void_p)]
+                ("device", C.c_int32), ("stream", C.c_void_p), ("panel_rows", C.c_uint64)]
 
 
+KKM_PANEL_AUTO = (1 << 64) - 1
 _LIB = None
 
 # Exported symbols with their ctypes signatures (restype, argtypes).
@@ -79,6 +80,7 @@ SIGNATURES = {
     "km_lloyd_set_data_bf16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "km_kkm_configure": (C.c_int, [C.c_void_p, C.c_uint64, C.c_float, C.c_int32]),
     "km_kkm_build_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "km_kkm_panel_rows": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     "km_lloyd_create": (C.c_int, [C.POINTER(LloydParams), C.POINTER(C.c_void_p)]),
     "km_lloyd_set_data": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "km_lloyd_fit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Result)]),
@@ -242,9 +244,14 @@ class KernelKMeans:
     """Handle over km_kkm_*: kernel k-means with the reference GPU path's semantics."""
 
     def __init__(self, n, d, k, kernel="linear", gamma=1.0, coef=1.0, degree=2, sigma=1.0, tol=1e-4,
-                 maxiter=30, precision="fp32", k_bf16=False, check_converged=False, device=0, stream=0):
+                 maxiter=30, precision="fp32", k_bf16=False, check_converged=False, device=0, stream=0,
+                 panel_rows=0):
+        """panel_rows: 0 keeps K resident (n*n); r > 0 rebuilds K every
+        iteration in panels of r rows; "auto" (KKM_PANEL_AUTO) picks panels only
+        when n*n does not fit the free device memory."""
+        pr = KKM_PANEL_AUTO if panel_rows == "auto" else int(panel_rows)
         self.p = KkmParams(n, d, k, tol, maxiter, KERNEL[kernel], gamma, coef, sigma, degree, PREC[precision],
-                           int(k_bf16), int(check_converged), device, stream or None)
+                           int(k_bf16), int(check_converged), device, stream or None, pr)
         h = C.c_void_p()
         check(_lib().km_kkm_create(C.byref(self.p), C.byref(h)), "km_kkm_create")
         self.h = h
@@ -262,6 +269,12 @@ class KernelKMeans:
         ms = C.c_double(0)
         check(_lib().km_kkm_build_ms(self.h, C.byref(ms)), "km_kkm_build_ms")
         return ms.value
+
+    def panel_rows(self):
+        """Rows of K per panel (0: K resident)."""
+        r = C.c_uint64(0)
+        check(_lib().km_kkm_panel_rows(self.h, C.byref(r)), "km_kkm_panel_rows")
+        return r.value
 
     def fit(self, init_labels=None):
         lab = np.empty(self.p.n, np.uint32)

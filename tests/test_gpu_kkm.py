@@ -112,3 +112,66 @@ def test_kkm_given_initial_labels_and_bad_labels(km, gpu):
         m.fit(init_labels=np.full(500, 9, np.uint32))
     assert e.value.status == km.KM_ERR_ARG
     m.close()
+
+
+def _fit(km, X, k, panel_rows, **kw):
+    n, d = X.shape
+    m = km.KernelKMeans(n, d, k, panel_rows=panel_rows, **kw).set_data(X)
+    lab, r = m.fit()
+    rows = m.panel_rows()
+    m.close()
+    return lab, r, rows
+
+
+@pytest.mark.parametrize("kb16", [False, True])
+@pytest.mark.parametrize("prec", ["fp32", "bf16x3", "bf16"])
+@pytest.mark.parametrize("kind,params", [("polynomial", dict(gamma=1 / 32, coef=1.0, degree=2)),
+                                         ("gaussian", dict(sigma=2.0))])
+def test_kkm_panels_equal_resident(km, gpu, kind, params, prec, kb16):
+    """K rebuilt every iteration in row panels (ragged last panel, panel rows
+    not a multiple of the 128-row tile, one panel of all rows) gives the same
+    K values in the same summation order as the resident matrix: labels,
+    score and iteration count are identical, including a fit that stops
+    early on the score rule with iterations still enqueued."""
+    X, _ = helpers.synth_blobs_np(3000, 32, 6, -1, 1, 0.35, 9)
+    kw = dict(kernel=kind, maxiter=12, tol=1e-3, precision=prec, k_bf16=kb16, check_converged=True, **params)
+    lab0, r0, rows0 = _fit(km, X, 6, 0, **kw)
+    assert rows0 == 0
+    for pr in (1000, 128, 3000, 5000):
+        lab, r, rows = _fit(km, X, 6, pr, **kw)
+        assert rows == min(pr, 3000)
+        np.testing.assert_array_equal(lab, lab0)
+        assert r.score == r0.score and r.iterations == r0.iterations
+        assert r.converged_iter == r0.converged_iter
+        panels = -(-3000 // rows)
+        # per enqueued iteration: 9 kernels resident; 8 + a build and a V.K per panel
+        assert r.kernel_launches == r0.kernel_launches // 9 * (8 + 2 * panels)
+
+
+def test_kkm_k256_global_labels_vs_oracle(km, gpu):
+    """k = 256 leaves no room for the n byte labels beside the V.K bins in
+    shared memory, so V.K reads them from a global byte copy (refreshed after
+    every iteration): against the FP64 oracle, resident and panelled."""
+    X, _ = helpers.synth_blobs_np(4096, 16, 256, -4, 4, 0.3, 21)
+    params = dict(gamma=1 / 16, coef=1.0, degree=2)
+    it_o, lab_o, sc_o, _ = oracle_kkm(X, "polynomial", params, 256, 6, 0.0, False)
+    for pr in (0, 1024):
+        lab, r, _ = _fit(km, X, 256, pr, kernel="polynomial", maxiter=6, precision="fp32", **params)
+        assert float((lab == lab_o).mean()) >= 0.998
+        assert abs(r.score - sc_o) <= 1e-4 * abs(sc_o)
+        assert r.iterations == 6
+
+
+def test_kkm_large_n_panels_equal_resident(km, gpu):
+    """n = 170,000 points: the byte labels (166 KiB) no longer fit beside the
+    bins of k = 64, which the resident path used to reject; BF16 K resident
+    (58 GB) and in panels of 8192 rows (2.8 GB) give identical fits."""
+    n, d, k = 170000, 32, 64
+    X, _ = helpers.synth_blobs_np(n, d, k, -1, 1, 0.3, 33)
+    kw = dict(kernel="gaussian", sigma=1.0, maxiter=3, precision="bf16", k_bf16=True)
+    lab0, r0, _ = _fit(km, X, k, 0, **kw)
+    lab1, r1, rows = _fit(km, X, k, 8192, **kw)
+    assert rows == 8192
+    np.testing.assert_array_equal(lab0, lab1)
+    assert r0.score == r1.score and r0.iterations == r1.iterations == 3
+    assert lab0.max() < k and np.isfinite(r0.score)

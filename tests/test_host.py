@@ -47,6 +47,15 @@ def test_argument_validation_without_device(km):
     p = km.LloydParams(100, 2, 3, float("nan"), 0, 10, 0, 0, 0, 0, None)
     assert lib.km_lloyd_create(C.byref(p), C.byref(h)) == km.KM_ERR_ARG
     assert lib.km_lloyd_fit(None, None, None, None, None) == km.KM_ERR_ARG
+    # kernel k-means, resident K and panels alike
+    for pr in (0, 512, km.KKM_PANEL_AUTO):
+        for n, d, k in ((10, 2, 11), (10, 0, 2), (0, 2, 1), (10, 2, 0)):
+            kp = km.KkmParams(n, d, k, 1e-4, 10, 1, 1.0, 1.0, 1.0, 2, 0, 0, 0, 0, None, pr)
+            assert lib.km_kkm_create(C.byref(kp), C.byref(h)) == km.KM_ERR_ARG
+        kp = km.KkmParams(1000, 4, 300, 1e-4, 10, 1, 1.0, 1.0, 1.0, 2, 0, 0, 0, 0, None, pr)   # k > 256
+        assert lib.km_kkm_create(C.byref(kp), C.byref(h)) == km.KM_ERR_UNSUPPORTED
+    r = C.c_uint64(0)
+    assert lib.km_kkm_panel_rows(None, C.byref(r)) == km.KM_ERR_ARG
 
 
 def test_no_device_is_reported_not_faked(km):
