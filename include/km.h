@@ -263,12 +263,18 @@ typedef struct km_kkm_params {
    * panel and streams each panel into E = K V^T, so memory is r*n instead
    * of n*n and n is no longer capped by n^2 bytes.  The panels hold the same
    * values as the resident matrix, so labels and score are identical.
-   * KM_KKM_PANEL_AUTO: resident when n*n fits in 90% of the free device
-   * memory, else panels sized to half of it. */
+   * KM_KKM_FUSED (tensor-core precisions): no K at all; every iteration
+   * multiplies X by a label-sorted copy of X on the tensor cores and sums
+   * each row's kernel values per cluster in the epilogue (memory n*d; labels
+   * within tolerance of the resident path, not bitwise: another summation
+   * order; k_bf16 does not apply).  KM_KKM_PANEL_AUTO: resident when n*n fits
+   * in 90% of the free device memory, else fused (tensor-core precisions) or
+   * panels sized to half of it (FP32). */
   uint64_t panel_rows;
 } km_kkm_params;
 
 #define KM_KKM_PANEL_AUTO UINT64_MAX
+#define KM_KKM_FUSED (UINT64_MAX - 1)
 
 km_status km_kkm_create(const km_kkm_params* p, km_kkm** out);
 /* Builds K from n*d points (host or device). */
@@ -276,7 +282,7 @@ km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device);
 /* Device time of the kernel-matrix build done by the last km_kkm_set_data
  * (with panels: only the operand preparation, K is built per iteration). */
 km_status km_kkm_build_ms(km_kkm* h, double* ms);
-/* Rows of K per panel chosen at create (0: K resident). */
+/* Rows of K per panel chosen at create (0: K resident, KM_KKM_FUSED: no K). */
 km_status km_kkm_panel_rows(km_kkm* h, uint64_t* rows);
 /* Changes maxiter, tol and the -c stop rule before the next fit. */
 km_status km_kkm_configure(km_kkm* h, uint64_t maxiter, float tol, int32_t check_converged);

@@ -390,6 +390,239 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
 }
 
 // ---------------------------------------------------------------------------
+// (c') E = K V^T without K in memory.  The columns of K are taken in
+// label-sorted order: the B operand is a copy of the points permuted by the
+// stable label sort (perm), so cluster c owns the contiguous columns
+// [cstart[c], cstart[c+1]) and E[i,c] is a running sum along row i of
+// f(x_i . x_perm(j)), j ascending.  Persistent CTAs take whole 128-row blocks
+// of K and sweep its 256-column tiles in order: warp 0 the TMA producer,
+// warp 1 the MMA issuer into two TMEM accumulators, warp 2 the TMEM
+// allocation, warps 4-7 the epilogue with one row per thread (TMEM lane
+// quadrant warp % 4).  Per 64-column chunk the epilogue applies f and, when no
+// cluster ends inside the chunk, adds the chunk's pairwise-tree sum to the
+// row's running sum; a chunk holding a boundary goes column by column through
+// a shared staging tile.  Each E[i,c] is written once, by its row's thread.
+// The order of the sum is fixed by the data (deterministic); it is not the
+// resident V.K kernel's lane-interleaved order.  Waits are bounded as in
+// kmat_tc_kernel.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr uint32_t KF_STG_BYTES = 4u * 64u * 32u * 4u;   // per epilogue warp: 64 columns x 32 rows
+
+struct KfSmem {
+  uint64_t full[8];
+  uint64_t empty[8];
+  uint64_t tfull[2];
+  uint64_t tempty[2];
+  uint64_t tdone;
+  uint32_t tmem_base;
+  int abort;
+};
+}  // namespace
+
+template <bool X3, int KIND>
+__global__ void __launch_bounds__(256, 1)
+kkm_fused_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tAlo,
+                    const __grid_constant__ CUtensorMap tB, const __grid_constant__ CUtensorMap tBlo,
+                    const float* __restrict__ xn2, const float* __restrict__ xn2p, uint64_t n, uint32_t KB,
+                    uint32_t S, KFn f, const uint32_t* __restrict__ cstart, uint32_t k, float* __restrict__ E,
+                    DevState* st) {
+  if (st->done) return;   // uniform over the grid: written by an earlier launch
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  const uint32_t stage_bytes = (KA_BYTES + KB_BYTES) * (X3 ? 2u : 1u);
+  float* stg_all = reinterpret_cast<float*>(smem + (size_t)S * stage_bytes);   // [4 warps][64][32]
+  KfSmem* ts = reinterpret_cast<KfSmem*>(smem + (size_t)S * stage_bytes + KF_STG_BYTES);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint64_t mt = (n + KM_M - 1) / KM_M, nt = (n + KM_N - 1) / KM_N;
+  if (threadIdx.x == 0) {
+    for (uint32_t s = 0; s < S; ++s) { mbar_init(&ts->full[s], 1); mbar_init(&ts->empty[s], 1); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], 4); }
+    mbar_init(&ts->tdone, 1);
+    ts->abort = 0;
+    mbar_fence_init();
+  }
+  if (warp == 2) tmem_alloc(&ts->tmem_base, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = ts->tmem_base;
+  volatile int* abort_flag = &ts->abort;
+  auto fail = [&](uint32_t where) {
+    ts->abort = 1;
+    if (atomicOr(&st->err, KM_DEVERR_TIMEOUT) == 0u) st->err_where = 110u + where;
+  };
+  if (warp == 0) {
+    if (lane == 0) {
+      uint64_t u = 0;
+      bool ok = true;
+      for (uint64_t mi = blockIdx.x; mi < mt && ok; mi += gridDim.x) {
+        for (uint64_t nj = 0; nj < nt && ok; ++nj) {
+          for (uint32_t kb = 0; kb < KB; ++kb, ++u) {
+            const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
+            if (!mbar_wait_bounded(&ts->empty[s], ph ^ 1u, abort_flag, KWAIT_NS)) { fail(1); ok = false; break; }
+            mbar_arrive_expect_tx(&ts->full[s], stage_bytes);
+            uint8_t* dst = smem + (size_t)s * stage_bytes;
+            tma_load_2d(dst, &tA, (int)(kb * 64), (int)(mi * KM_M), &ts->full[s]);
+            tma_load_2d(dst + KA_BYTES, &tB, (int)(kb * 64), (int)(nj * KM_N), &ts->full[s]);
+            if (X3) {
+              tma_load_2d(dst + KA_BYTES + KB_BYTES, &tAlo, (int)(kb * 64), (int)(mi * KM_M), &ts->full[s]);
+              tma_load_2d(dst + 2 * KA_BYTES + KB_BYTES, &tBlo, (int)(kb * 64), (int)(nj * KM_N), &ts->full[s]);
+            }
+          }
+        }
+      }
+      volatile int no_abort = 0;
+      const uint64_t first = u > S ? u - S : 0;
+      for (uint64_t v = first; v < u; ++v)
+        mbar_wait_bounded(&ts->full[v % S], (uint32_t)((v / S) & 1u), &no_abort, KWAIT_NS);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(KM_M, KM_N);
+      const uint32_t s0 = smem_u32(smem);
+      uint64_t u = 0, t = 0;
+      bool ok = true, issued = false;
+      for (uint64_t mi = blockIdx.x; mi < mt && ok; mi += gridDim.x) {
+        for (uint64_t nj = 0; nj < nt && ok; ++nj, ++t) {
+          const uint32_t buf = (uint32_t)(t & 1u), use = (uint32_t)(t >> 1);
+          if (!mbar_wait_bounded(&ts->tempty[buf], (use & 1u) ^ 1u, abort_flag, KWAIT_NS)) { fail(2); ok = false; break; }
+          tc_fence_after();
+          const uint32_t dt = tmem_base + buf * 256u;
+          for (uint32_t kb = 0; kb < KB; ++kb, ++u) {
+            const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
+            if (!mbar_wait_bounded(&ts->full[s], ph, abort_flag, KWAIT_NS)) { fail(3); ok = false; break; }
+            tc_fence_after();
+            const uint32_t a0 = s0 + s * stage_bytes, b0 = a0 + KA_BYTES;
+#pragma unroll
+            for (uint32_t kk = 0; kk < 4; ++kk) {
+              const uint64_t ad = smem_desc_sw128(a0 + kk * 32u);
+              const uint64_t bd = smem_desc_sw128(b0 + kk * 32u);
+              tc_mma_bf16(dt, ad, bd, idesc, (kb | kk) != 0u ? 1u : 0u);
+              if (X3) {
+                const uint64_t adl = smem_desc_sw128(a0 + KA_BYTES + KB_BYTES + kk * 32u);
+                const uint64_t bdl = smem_desc_sw128(a0 + 2 * KA_BYTES + KB_BYTES + kk * 32u);
+                tc_mma_bf16(dt, ad, bdl, idesc, 1u);
+                tc_mma_bf16(dt, adl, bd, idesc, 1u);
+              }
+            }
+            tc_commit(&ts->empty[s]);
+            issued = true;
+          }
+          if (!ok) break;
+          tc_commit(&ts->tfull[buf]);
+        }
+      }
+      if (issued) {
+        tc_commit(&ts->tdone);
+        volatile int no_abort = 0;
+        mbar_wait_bounded(&ts->tdone, 0, &no_abort, KWAIT_NS);
+      }
+    }
+  } else if (warp >= 4) {
+    const int q = warp & 3;
+    const uint32_t tq = tmem_base + (((uint32_t)q * 32u) << 16);
+    float* stg = stg_all + (size_t)q * 64 * 32;
+    auto colnorm = [&](uint64_t j) -> float {
+      return (KIND == KM_KERNEL_GAUSSIAN) ? __ldg(xn2p + j) : 0.0f;
+    };
+    uint64_t t = 0;
+    bool ok = true;
+    for (uint64_t mi = blockIdx.x; mi < mt && ok; mi += gridDim.x) {
+      const uint64_t row = mi * KM_M + (uint64_t)q * 32u + (uint64_t)lane;
+      const bool valid = row < n;
+      const float ni = (KIND == KM_KERNEL_GAUSSIAN && valid) ? xn2[row] : 0.0f;
+      float* Er = E + row * k;
+      uint32_t cur = 0;                 // cluster of the running sum
+      uint64_t nb = cstart[1];          // first column after cluster cur
+      float run = 0.0f;
+      for (uint64_t nj = 0; nj < nt; ++nj, ++t) {
+        const uint32_t buf = (uint32_t)(t & 1u);
+        const bool okw = mbar_wait_bounded(&ts->tfull[buf], (uint32_t)(t >> 1) & 1u, abort_flag, KWAIT_NS);
+        if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(4); ok = false; break; }
+        tc_fence_after();
+        for (uint32_t pr = 0; pr < KM_N / 64; ++pr) {
+          const uint64_t j0 = nj * KM_N + pr * 64u;
+          if (j0 >= n) break;                                   // warp-uniform
+          uint32_t acc[64];
+          tmem_ld_32x32b_x64(tq + buf * 256u + pr * 64u, acc);
+          tmem_ld_wait();
+          if (nb >= j0 + 64 && j0 + 64 <= n) {
+            float v[64];
+#pragma unroll
+            for (int c = 0; c < 64; ++c) v[c] = kfn_apply_k<KIND>(f, __uint_as_float(acc[c]), ni, colnorm(j0 + c));
+#pragma unroll
+            for (int w = 32; w >= 1; w >>= 1)
+#pragma unroll
+              for (int c = 0; c < w; ++c) v[c] += v[c + w];
+            run += v[0];
+          } else {
+            // a cluster ends inside this chunk (or the points do): column by column
+#pragma unroll
+            for (int c = 0; c < 64; ++c)
+              stg[c * 32 + lane] = (j0 + c < n) ? kfn_apply_k<KIND>(f, __uint_as_float(acc[c]), ni, colnorm(j0 + c))
+                                                : 0.0f;
+            __syncwarp();
+            const uint32_t cols = (uint32_t)((n - j0) < 64 ? (n - j0) : 64);
+#pragma unroll 1
+            for (uint32_t c = 0; c < cols; ++c) {
+              const uint64_t j = j0 + c;
+              while (j == nb) {                                 // cluster cur ended before column j
+                if (valid) Er[cur] = run;
+                run = 0.0f;
+                ++cur;
+                nb = cstart[cur + 1];
+              }
+              run += stg[c * 32 + lane];
+            }
+            __syncwarp();
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&ts->tempty[buf]);
+      }
+      if (!ok) break;
+      // the last non-empty cluster, then the empty ones after it
+      for (; cur < k; ++cur) {
+        if (valid) Er[cur] = run;
+        run = 0.0f;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 2) tmem_dealloc(tmem_base, 512);
+}
+
+// Label-sorted copies of the tensor-core operands and of their norms: row j of
+// a copy is row perm[j] of the original.  One warp per row, 16-byte copies
+// (dp is a multiple of 64).
+__global__ void kkm_permute_points_kernel(const __nv_bfloat16* __restrict__ Xb,
+                                          const __nv_bfloat16* __restrict__ Xlo, const float* __restrict__ xn2,
+                                          const uint32_t* __restrict__ perm, uint64_t n, uint32_t dp,
+                                          __nv_bfloat16* __restrict__ Xbp, __nv_bfloat16* __restrict__ Xlop,
+                                          float* __restrict__ xn2p, const DevState* st) {
+  if (st->done) return;
+  const uint64_t j = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (j >= n) return;
+  const uint64_t src = perm[j];
+  const uint32_t w16 = dp / 8;
+  const uint4* a = reinterpret_cast<const uint4*>(Xb + src * dp);
+  uint4* b = reinterpret_cast<uint4*>(Xbp + j * dp);
+  for (uint32_t w = lane; w < w16; w += 32) b[w] = __ldg(a + w);
+  if (Xlo) {
+    const uint4* al = reinterpret_cast<const uint4*>(Xlo + src * dp);
+    uint4* bl = reinterpret_cast<uint4*>(Xlop + j * dp);
+    for (uint32_t w = lane; w < w16; w += 32) bl[w] = __ldg(al + w);
+  }
+  if (lane == 0) xn2p[j] = xn2[src];
+}
+
+// ---------------------------------------------------------------------------
 // (c) E = K V^T.  One warp per row of K at a time; the labels of all n points
 // are bytes (k <= 256), in shared memory when they fit next to the bins
 // (GLAB false) or else read from a global byte copy (GLAB true, L2-resident);
@@ -607,6 +840,15 @@ struct km_kkm {
   uint8_t* lab8 = nullptr;  // byte labels for the V.K kernel when they do not fit shared memory
   bool glab = false;
   uint64_t kpi = 0;         // kernels launched per iteration
+  // fused mode (no K): label-sorted operand copies and the fused kernel's plan
+  bool fused = false;
+  __nv_bfloat16* Xbp = nullptr;
+  __nv_bfloat16* Xlop = nullptr;
+  float* xn2p = nullptr;
+  CUtensorMap fA{}, fAlo{}, fB{}, fBlo{};
+  uint32_t fS = 0;
+  size_t fsmem = 0;
+  int fgrid = 0;
   float* E = nullptr;       // n x k
   double* ct = nullptr;
   uint32_t* lab = nullptr;  // current labels
@@ -719,9 +961,93 @@ km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32
 }
 
 // Per iteration: V.K (with the K panel builds before each panel's V.K when
-// K is not resident), 4 sort kernels, c~, distances/argmin, control, label copy.
-uint64_t kkm_kernels_per_iter(uint64_t n, uint64_t panel) {
+// K is not resident), 4 sort kernels, c~, distances/argmin, control, label
+// copy; fused: the sort, the operand permutation and the fused kernel
+// instead of V.K.
+uint64_t kkm_kernels_per_iter(uint64_t n, uint64_t panel, bool fused) {
+  if (fused) return 10;
   return panel ? 8 + 2 * ((n + panel - 1) / panel) : 9;
+}
+
+template <bool X3, int KIND>
+km_status kkm_fused_attr(size_t smem) {
+  KM_CUDA_TRY(cudaFuncSetAttribute(kkm_fused_tc_kernel<X3, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  return KM_OK;
+}
+
+template <bool X3>
+km_status kkm_fused_attr_kind(int kind, size_t smem) {
+  switch (kind) {
+    case KM_KERNEL_LINEAR: return kkm_fused_attr<X3, KM_KERNEL_LINEAR>(smem);
+    case KM_KERNEL_POLY: return kkm_fused_attr<X3, KM_KERNEL_POLY>(smem);
+    case KM_KERNEL_SIGMOID: return kkm_fused_attr<X3, KM_KERNEL_SIGMOID>(smem);
+    default: return kkm_fused_attr<X3, KM_KERNEL_GAUSSIAN>(smem);
+  }
+}
+
+// Operand copies, tensor maps and launch shape of the fused kernel.
+km_status kkm_fused_plan(km_kkm* h) {
+  LloydEngine& e = h->eng;
+  const uint64_t n = h->p.n;
+  const bool x3 = h->p.precision == KM_PREC_BF16X3;
+  if (cudaMalloc(&h->Xbp, sizeof(__nv_bfloat16) * n * e.dp) != cudaSuccess ||
+      (x3 && cudaMalloc(&h->Xlop, sizeof(__nv_bfloat16) * n * e.dp) != cudaSuccess) ||
+      cudaMalloc(&h->xn2p, sizeof(float) * n) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return KM_ERR_ALLOC;
+  }
+  KM_TRY(encode_tmap_bf16(&h->fA, e.Xb, e.dp, n, 64, KM_M));
+  KM_TRY(encode_tmap_bf16(&h->fB, h->Xbp, e.dp, n, 64, KM_N));
+  if (x3) {
+    KM_TRY(encode_tmap_bf16(&h->fAlo, e.Xlo, e.dp, n, 64, KM_M));
+    KM_TRY(encode_tmap_bf16(&h->fBlo, h->Xlop, e.dp, n, 64, KM_N));
+  } else {
+    h->fAlo = h->fA;
+    h->fBlo = h->fB;
+  }
+  const size_t stage = (size_t)(KA_BYTES + KB_BYTES) * (x3 ? 2 : 1);
+  const size_t fixed = 1024 + KF_STG_BYTES + sizeof(KfSmem) + 64;
+  size_t S = (227 * 1024 - fixed) / stage;
+  if (S > 8) S = 8;
+  if (S < 2) return KM_ERR_UNSUPPORTED;
+  h->fS = (uint32_t)S;
+  h->fsmem = fixed + S * stage;
+  h->fgrid = (int)std::min<uint64_t>((n + KM_M - 1) / KM_M, (uint64_t)e.num_sms);
+  if (x3) KM_TRY(kkm_fused_attr_kind<true>(h->p.kernel_fn, h->fsmem));
+  else KM_TRY(kkm_fused_attr_kind<false>(h->p.kernel_fn, h->fsmem));
+  return KM_OK;
+}
+
+km_status kkm_launch_fused(km_kkm* h) {
+  LloydEngine& e = h->eng;
+  const uint64_t n = h->p.n;
+  const bool x3 = h->p.precision == KM_PREC_BF16X3;
+  cudaStream_t s = e.stream;
+  kkm_permute_points_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(
+      e.Xb, x3 ? e.Xlo : nullptr, e.xn2, e.perm, n, e.dp, h->Xbp, h->Xlop, h->xn2p, e.st);
+  KM_CUDA_TRY(cudaGetLastError());
+  const KFn f = make_kfn(h->p);
+  const uint32_t KBn = e.dp / 64;
+#define KM_LAUNCH_FUSED(X3_, KIND_)                                                                \
+  kkm_fused_tc_kernel<X3_, KIND_><<<h->fgrid, 256, h->fsmem, s>>>(h->fA, h->fAlo, h->fB, h->fBlo,  \
+                                                                  e.xn2, h->xn2p, n, KBn, h->fS,   \
+                                                                  f, e.cstart, h->p.k, h->E, e.st)
+#define KM_LAUNCH_FUSED_KIND(X3_)                                                                  \
+  do {                                                                                             \
+    switch (f.kind) {                                                                              \
+      case KM_KERNEL_LINEAR: KM_LAUNCH_FUSED(X3_, KM_KERNEL_LINEAR); break;                        \
+      case KM_KERNEL_POLY: KM_LAUNCH_FUSED(X3_, KM_KERNEL_POLY); break;                            \
+      case KM_KERNEL_SIGMOID: KM_LAUNCH_FUSED(X3_, KM_KERNEL_SIGMOID); break;                      \
+      default: KM_LAUNCH_FUSED(X3_, KM_KERNEL_GAUSSIAN); break;                                    \
+    }                                                                                              \
+  } while (0)
+  if (x3) KM_LAUNCH_FUSED_KIND(true);
+  else KM_LAUNCH_FUSED_KIND(false);
+#undef KM_LAUNCH_FUSED_KIND
+#undef KM_LAUNCH_FUSED
+  KM_CUDA_TRY(cudaGetLastError());
+  return KM_OK;
 }
 
 km_status kkm_launch_vk(km_kkm* h, uint64_t r0, uint64_t r1) {
@@ -746,7 +1072,12 @@ km_status kkm_enqueue_iteration(km_kkm* h, const LoopConsts& lc) {
   const uint64_t n = h->p.n;
   const uint32_t k = h->p.k;
   cudaStream_t s = e.stream;
-  if (h->panel) {
+  if (h->fused) {
+    // no K: the label sort first (its permutation orders the columns), then
+    // the fused K.V^T
+    KM_TRY(e.enqueue_sort(h->lab));
+    KM_TRY(kkm_launch_fused(h));
+  } else if (h->panel) {
     // K is not resident: rebuild it panel by panel, each panel streamed into
     // its rows of E before the next one overwrites it (stream order)
     const KFn f = make_kfn(h->p);
@@ -759,7 +1090,7 @@ km_status kkm_enqueue_iteration(km_kkm* h, const LoopConsts& lc) {
   } else {
     KM_TRY(kkm_launch_vk(h, 0, n));
   }
-  KM_TRY(e.enqueue_sort(h->lab));
+  if (!h->fused) KM_TRY(e.enqueue_sort(h->lab));
   kkm_ctilde_kernel<<<(k * 32 + 255) / 256, 256, 0, s>>>(h->E, k, e.perm, e.cstart, h->ct, e.st);
   kkm_dist_kernel<<<h->dist_blocks, 256, 2 * k * sizeof(float), s>>>(h->E, n, k, e.counts, h->ct, h->nlab,
                                                                       h->part, e.st);
@@ -832,23 +1163,38 @@ km_status km_kkm_create(const km_kkm_params* p, km_kkm** out) {
     (void)cudaGetLastError();
     return fail(KM_ERR_ALLOC);
   }
-  // K last: resident (n x n) or one panel of rows
+  // K last: resident (n x n), one panel of rows, or none (fused)
   const size_t bpe = p->k_bf16 ? 2 : 4;
+  const bool tensor = p->precision != KM_PREC_FP32;
   uint64_t panel = 0;
-  if (p->panel_rows == KM_KKM_PANEL_AUTO) {
+  bool fused = false;
+  if (p->panel_rows == KM_KKM_FUSED) {
+    if (!tensor) return fail(KM_ERR_UNSUPPORTED);
+    fused = true;
+  } else if (p->panel_rows == KM_KKM_PANEL_AUTO) {
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { (void)cudaGetLastError(); return fail(KM_ERR_CUDA); }
     if ((double)nn * bpe > 0.9 * (double)fr) {
-      const uint64_t r = (uint64_t)(0.5 * (double)fr / ((double)p->n * bpe)) / 128 * 128;
-      panel = std::min<uint64_t>(std::max<uint64_t>(r, 128), p->n);
+      if (tensor) {
+        fused = true;
+      } else {
+        const uint64_t r = (uint64_t)(0.5 * (double)fr / ((double)p->n * bpe)) / 128 * 128;
+        panel = std::min<uint64_t>(std::max<uint64_t>(r, 128), p->n);
+      }
     }
   } else if (p->panel_rows > 0) {
     panel = std::min<uint64_t>(p->panel_rows, p->n);
   }
   h->panel = panel;
-  h->kpi = kkm_kernels_per_iter(p->n, panel);
-  const size_t kbytes = (panel ? panel * p->n : nn) * bpe;
-  if (cudaMalloc(&h->K, kbytes) != cudaSuccess) { (void)cudaGetLastError(); return fail(KM_ERR_ALLOC); }
+  h->fused = fused;
+  h->kpi = kkm_kernels_per_iter(p->n, panel, fused);
+  if (fused) {
+    s = kkm_fused_plan(h);
+    if (s != KM_OK) return fail(s);
+  } else {
+    const size_t kbytes = (panel ? panel * p->n : nn) * bpe;
+    if (cudaMalloc(&h->K, kbytes) != cudaSuccess) { (void)cudaGetLastError(); return fail(KM_ERR_ALLOC); }
+  }
   h->dist_blocks = (int)std::min<uint64_t>((p->n + 255) / 256, 1024);
   bool attr_ok = true;
   if (glab) {
@@ -878,8 +1224,8 @@ km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device) {
   const KFn f = make_kfn(h->p);
   KM_CUDA_TRY(cudaEventRecord(h->ev0, e.stream));
   KM_TRY(prepare_kmat_norms(e, h->p.n, f, h->p.precision));
-  // with panels, K is built inside every iteration instead
-  if (!h->panel)
+  // with panels (or fused), K is built inside every iteration instead
+  if (!h->panel && !h->fused)
     KM_TRY(build_kernel_matrix(e, e.X, h->p.n, h->p.d, f, h->p.precision, h->p.k_bf16 != 0, h->K, h->diag, 0,
                                h->p.n, false));
   KM_CUDA_TRY(cudaEventRecord(h->ev1, e.stream));
@@ -894,7 +1240,7 @@ km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device) {
 
 km_status km_kkm_panel_rows(km_kkm* h, uint64_t* rows) {
   if (!h || !rows) return KM_ERR_ARG;
-  *rows = h->panel;
+  *rows = h->fused ? KM_KKM_FUSED : h->panel;
   return KM_OK;
 }
 
@@ -976,6 +1322,9 @@ void km_kkm_destroy(km_kkm* h) {
   if (h->lab) cudaFree(h->lab);
   if (h->nlab) cudaFree(h->nlab);
   if (h->lab8) cudaFree(h->lab8);
+  if (h->Xbp) cudaFree(h->Xbp);
+  if (h->Xlop) cudaFree(h->Xlop);
+  if (h->xn2p) cudaFree(h->xn2p);
   if (h->part) cudaFree(h->part);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);

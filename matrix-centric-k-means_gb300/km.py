@@ -54,6 +54,7 @@ class KkmParams(C.Structure):
 
 
 KKM_PANEL_AUTO = (1 << 64) - 1
+KKM_FUSED = (1 << 64) - 2
 _LIB = None
 
 # Exported symbols with their ctypes signatures (restype, argtypes).
@@ -247,9 +248,12 @@ class KernelKMeans:
                  maxiter=30, precision="fp32", k_bf16=False, check_converged=False, device=0, stream=0,
                  panel_rows=0):
         """panel_rows: 0 keeps K resident (n*n); r > 0 rebuilds K every
-        iteration in panels of r rows; "auto" (KKM_PANEL_AUTO) picks panels only
-        when n*n does not fit the free device memory."""
-        pr = KKM_PANEL_AUTO if panel_rows == "auto" else int(panel_rows)
+        iteration in panels of r rows; "fused" (KKM_FUSED) keeps no K and sums
+        the kernel values per cluster inside the tensor-core kernel; "auto"
+        (KKM_PANEL_AUTO) leaves K resident when n*n fits the free device
+        memory, else fused (tensor-core precisions) or panels (FP32)."""
+        pr = {"auto": KKM_PANEL_AUTO, "fused": KKM_FUSED}.get(panel_rows, panel_rows)
+        pr = int(pr)
         self.p = KkmParams(n, d, k, tol, maxiter, KERNEL[kernel], gamma, coef, sigma, degree, PREC[precision],
                            int(k_bf16), int(check_converged), device, stream or None, pr)
         h = C.c_void_p()
@@ -271,7 +275,7 @@ class KernelKMeans:
         return ms.value
 
     def panel_rows(self):
-        """Rows of K per panel (0: K resident)."""
+        """Rows of K per panel (0: K resident, KKM_FUSED: no K)."""
         r = C.c_uint64(0)
         check(_lib().km_kkm_panel_rows(self.h, C.byref(r)), "km_kkm_panel_rows")
         return r.value
