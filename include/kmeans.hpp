@@ -70,7 +70,9 @@ class Kmeans {
   // Extension: arithmetic of the distance stage (linear) or of the K build.
   // automatic: split-BF16x3 tensor cores with exact re-scoring for the linear
   // kernel (labels identical to fp32, several times faster), fp32 for the K
-  // build of the other kernels (K then matches an FP32 build).
+  // build of the other kernels (K then matches an FP32 build) while the n*n
+  // FP32 kernel matrix fits the device; beyond that, where an n*n buffer
+  // cannot exist, split-BF16x3 without a stored K (the fused kernel).
   enum class Precision { fp32, bf16, bf16x3, automatic };
 
   using KernelParams = KmeansKernelParams;

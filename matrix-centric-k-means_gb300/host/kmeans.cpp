@@ -82,6 +82,13 @@ void Kmeans::setup(const float* X, const int* seed, InitMethod initMethod, Kerne
     p.sigma = kp.sigma;
     p.degree = kp.degree;
     p.precision = to_prec(precision, kernel == Kernel::linear);
+    if (precision == Precision::automatic) {
+      // an FP32 n*n kernel matrix that does not fit the device: no stored K
+      // (fused split-BF16x3) instead of rebuilding FP32 panels every iteration
+      uint64_t fr = 0, tot = 0;
+      if (km_mem_info(0, &fr, &tot) == KM_OK && (double)n * (double)n * 4.0 > 0.9 * (double)fr)
+        p.precision = KM_PREC_BF16X3;
+    }
     p.k_bf16 = 0;
     p.check_converged = 0;
     p.device = 0;
