@@ -27,6 +27,53 @@ def test_library_exports_every_declared_symbol(km):
     assert set(names) == set(km.SIGNATURES), "km.py signatures out of sync with km.h"
 
 
+C_TYPES = {"uint64_t": "c_ulong", "uint32_t": "c_uint", "int32_t": "c_int", "float": "c_float",
+           "double": "c_double", "void*": "c_void_p"}
+
+
+def declared_structs():
+    """{name: [(field, c type), ...]} of the plain structs km.h defines."""
+    src = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    out = {}
+    for name, body in re.findall(r"typedef struct (km_\w+) \{(.*?)\} \1;", src, flags=re.S):
+        fields = []
+        for decl in body.split(";"):
+            decl = decl.strip()
+            if not decl:
+                continue
+            m = re.match(r"(\w+\s*\*?)\s*(.+)", decl)
+            ctype = m.group(1).replace(" ", "")
+            for f in m.group(2).split(","):
+                f = f.strip()
+                if f.startswith("*"):
+                    ctype, f = ctype + "*", f[1:].strip()
+                fields.append((f, ctype))
+        out[name] = fields
+    return out
+
+
+def test_ctypes_structures_match_the_header(km):
+    """Every structure km.py passes through the ABI has the header's fields,
+    in the header's order, with the same C types (a drift would shift fields
+    silently), and the kernel k-means mode constants agree."""
+    import ctypes as C
+    pairs = {"km_lloyd_params": km.LloydParams, "km_result": km.Result, "km_kkm_params": km.KkmParams,
+             "km_batch_problem": km.BatchProblem, "km_batch_params": km.BatchParams,
+             "km_batch_result": km.BatchResult}
+    structs = declared_structs()
+    assert set(pairs) <= set(structs), set(pairs) - set(structs)
+    for cname, py in pairs.items():
+        want = structs[cname]
+        got = [(f, t.__name__) for f, t in py._fields_]
+        assert [f for f, _ in got] == [f for f, _ in want], cname
+        for (f, t), (_, ct) in zip(got, want):
+            exp = getattr(C, C_TYPES[ct]).__name__
+            assert t == exp, (cname, f, t, ct)
+    src = HEADER.read_text()
+    assert "#define KM_KKM_PANEL_AUTO UINT64_MAX" in src and km.KKM_PANEL_AUTO == 2 ** 64 - 1
+    assert "#define KM_KKM_FUSED (UINT64_MAX - 1)" in src and km.KKM_FUSED == 2 ** 64 - 2
+
+
 def test_status_strings(km):
     lib = km.lib()
     for s in range(8):
