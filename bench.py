@@ -112,6 +112,17 @@ class Clocks:
                 "samples": len(self.rows)}
 
 
+def repo_libraries_loaded():
+    """Shared libraries of this repository mapped into this process (from
+    /proc/self/maps; empty where that file does not exist)."""
+    try:
+        maps = Path("/proc/self/maps").read_text().splitlines()
+    except OSError:
+        return []
+    libs = {ln.split()[-1] for ln in maps if ln.endswith(".so") and str(ROOT) in ln}
+    return sorted(str(Path(x).relative_to(ROOT)) for x in libs)
+
+
 def bench_config(world):
     """The `config` object both arms print."""
     return {"workload": f"lloyd n={N} d={D} k={K} (256 gaussian blobs, sigma 1, centers U[-10,10])",
@@ -151,6 +162,42 @@ def run_cpu_sample(X, threads, sample_rows, min_seconds, use_ref=False):
     return 1.0 / per_iter_full, statistics.median(t), len(t)
 
 
+PARITY_ITERS = 5        # iterations of the full-size oracle comparison
+
+
+def oracle_parity(km, X, Xd, dev, stream, precisions):
+    """Full-size parity with the oracle on the bench's own points: a
+    PARITY_ITERS-iteration fit per precision (seeded sample-pick init, the
+    reference CPU's centroid-shift stop rule with tol) against
+    (1) the oracle's restatement of the reference CPU k-means
+        (comparisons/CPU_Kmeans/src/kmeans.cpp:49-200): labels and centroids
+        bit for bit and the returned iteration;
+    (2) the FP64 oracle from the same initial centroids: label agreement and
+        the relative error of the last assignment's objective."""
+    import torch
+    import helpers
+    threads = os.cpu_count() or 8
+    t0 = time.perf_counter()
+    it32, lab32, cen32, _ = helpers.orc_lloyd(X, K, TOL, KM_SEED, PARITY_ITERS, threads=threads)
+    it64, lab64, _, _, obj64 = helpers.orc_lloyd64_obj(X, K, TOL, KM_SEED, PARITY_ITERS, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    out = {"iterations": PARITY_ITERS, "oracle_seconds": cpu_s, "oracle_threads": threads}
+    with torch.cuda.stream(stream):
+        for prec in precisions:
+            m = km.Lloyd(N, D, K, tol=TOL, seed=KM_SEED, maxiter=PARITY_ITERS, precision=prec, conv="shift",
+                         device=dev, stream=stream.cuda_stream).set_data(Xd)
+            lab, cen, r = m.fit()
+            m.close()
+            out[prec] = {
+                "label_agreement_vs_oracle": float((lab == lab32).mean()),
+                "centroids_bitwise_equal_vs_oracle": bool(np.array_equal(cen.view(np.uint32), cen32.view(np.uint32))),
+                "iteration_equal_vs_oracle": int(r.converged_iter) == it32,
+                "label_agreement_vs_fp64": float((lab == lab64).mean()),
+                "objective_rel_err_vs_fp64": abs(r.objective - obj64) / abs(obj64),
+            }
+    return out
+
+
 def reference_arm(args, rank):
     import helpers
     if rank != 0:
@@ -162,7 +209,9 @@ def reference_arm(args, rank):
     # the port runs one whole iteration over all n points per step; the
     # single-threaded reference build (about 30 s per full iteration) a 1/16 slice
     sample = N if not use_ref else N // 16
-    X = make_data(helpers.km())
+    # the numpy twin of the product's generator (same values, checked in the
+    # CPU tests), so that this arm loads no product library
+    X, _ = helpers.synth_blobs_np_chunked(N, D, BLOBS, LO, HI, SIGMA, DATA_SEED)
     vals = []
     for i in range(args.warmup + args.steps):
         v, secs, _ = run_cpu_sample(X, threads, sample, 0.0, use_ref)
@@ -183,6 +232,7 @@ def reference_arm(args, rank):
                                    f"k={K} centroids per step on {threads} host threads"
                                    + (f", scaled by n/{sample}" if sample != N else "")},
         "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "repo_libraries_loaded": repo_libraries_loaded(),
     }
     return line
 
@@ -250,7 +300,10 @@ def ours_arm(args, rank, world):
     names = ["distance+argmin", "refine", "label sort", "centroid sums", "finalize+control"]
     hbm, bf16, src = peaks()
     dp = (D + 63) // 64 * 64
-    # algorithmic bytes of each stage per iteration
+    # algorithmic bytes of each stage per iteration: distance = BF16 point
+    # copies (hi, and lo for the split form) + labels + minima; sort = labels
+    # read three times + the permutation written; sums = X + permutation +
+    # centroids in and out; finalize = three passes over k x d floats
     bytes_stage = [N * dp * 2 + N * 4 + N * 4, 0, 3 * N * 4 + N * 4,
                    N * D * 4 + N * 4 + 2 * K * D * 4, K * D * 4 * 3]
     if args.precision == "bf16x3":
@@ -270,6 +323,8 @@ def ours_arm(args, rank, world):
         ach_gb = bytes_stage[dom] / (st_ms / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": ach_gb, "peak": hbm, "unit": "GB/s", "frac": ach_gb / hbm}
     roof.update({"kernel": names[dom], "ms": st_ms, "peak_source": src,
+                 "ms_source": "km_lloyd_profile: one iteration captured as a CUDA graph with event-record "
+                              "nodes between the stages, replayed on the launching stream",
                  "traffic": TRAFFIC.get((args.precision, names[dom]))})
 
     # e2e: the public C ABI from pinned host memory: set_data (H2D) + fit + labels D2H,
@@ -292,10 +347,15 @@ def ours_arm(args, rank, world):
                 torch.cuda.synchronize()
                 wall = time.perf_counter() - t0
             m.close()
-        e2e = {"value": r.iterations / wall, "unit": "iters/s", "h2d_bytes_per_step": N * D * 4,
-               "d2h_bytes_per_step": N * 4,
+        its = max(1, r.iterations)
+        e2e = {"value": r.iterations / wall, "unit": "iters/s",
+               "h2d_bytes_per_step": N * D * 4 / its, "d2h_bytes_per_step": N * 4 / its,
+               "h2d_bytes_per_fit": N * D * 4, "d2h_bytes_per_fit": N * 4,
                "step": f"one km_lloyd_fit from pinned host memory: km_lloyd_set_data (H2D of X) + "
-                       f"seeded init + {r.iterations} iterations + labels D2H; wall clock {wall * 1e3:.2f} ms"}
+                       f"seeded init + {r.iterations} iterations + labels D2H; wall clock {wall * 1e3:.2f} ms; "
+                       f"the fit's copies divided over its {r.iterations} iterations"}
+
+    parity = oracle_parity(km, X, Xd, dev, stream, [args.precision, "fp32"] + others) if rank == 0 else None
 
     cpu = None
     if rank == 0:
@@ -320,6 +380,9 @@ def ours_arm(args, rank, world):
                            for q in others},
         "speedup_vs_fp32_plain": value / world / fp32_ips,
         "label_agreement_vs_fp32": agree,
+        "label_agreement_vs_oracle": parity[args.precision]["label_agreement_vs_oracle"] if parity else None,
+        "objective_rel_err_vs_fp64": parity[args.precision]["objective_rel_err_vs_fp64"] if parity else None,
+        "oracle_parity": parity,
         "refined_rows_per_iter": timing[args.precision]["refined"] / max(1, iters),
         "full_rescore_rows_per_iter": timing[args.precision]["full"] / max(1, iters),
         "objective": timing[args.precision]["objective"],

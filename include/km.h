@@ -177,7 +177,9 @@ km_status km_lloyd_device_results(km_lloyd* h, const uint32_t** labels_dev,
 
 /* Stage timing (the reference's [PERFORMANCE] lines, src/kmeans.cu:837-1048):
  * continues from the state of the last fit for `iters` more iterations, without
- * the stop rule, with CUDA events between the stages on the handle's stream, and
+ * the stop rule.  One iteration (the fit's kernels) is captured as a CUDA graph
+ * with event-record nodes between the stages and replayed `iters` times on the
+ * handle's stream (launched directly, stage by stage, if the capture fails);
  * writes the mean milliseconds per iteration of each stage to stage_ms[0..4]:
  * 0 distance+argmin, 1 near-tie refinement, 2 label sort (V), 3 centroid sums
  * (V.X), 4 finalize + loop control.  Labels and centroids advance as in a fit. */
@@ -223,10 +225,16 @@ km_status km_update(const float* X_dev, const uint32_t* labels_dev, uint64_t n, 
  * allocating routine.  Limits: n <= KM_NOALLOC_MAX_N and k <= KM_NOALLOC_MAX_K;
  * larger sizes return KM_ERR_UNSUPPORTED before any work.  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress, with that
- * device current); make that first call before any stream capture.  Every call
- * shares the array and the call clears what must start at zero: calls that
- * overlap on the GPU (other streams or host threads) race and must not be
- * issued.  counts_dev may be NULL. */
+ * device current); with CUDA's lazy module loading that is also when the array
+ * is placed on the device, so make the first call before a pool claims the
+ * device's memory (or set CUDA_MODULE_LOADING=EAGER).  Every call shares the
+ * array and the call clears what must start at zero: calls that overlap on the
+ * GPU (other streams or host threads) race and must not be issued.
+ * The call enqueues all of its work on `stream`, then synchronises that stream
+ * once, at the end, to read the error bits back; so it blocks the host until
+ * the update is done, and it cannot be used while the stream is being captured.
+ * Labels >= k return KM_ERR_ARG (C_dev is then undefined), a device wait that
+ * ran out KM_ERR_TIMEOUT.  counts_dev may be NULL. */
 #define KM_NOALLOC_MAX_N 1048576u
 #define KM_NOALLOC_MAX_K 1024u
 #define KM_NOALLOC_SCRATCH_BYTES 5505024u

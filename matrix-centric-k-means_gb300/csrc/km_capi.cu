@@ -345,20 +345,44 @@ km_status km_lloyd_profile(km_lloyd* h, uint64_t iters, double* stage_ms) {
   LoopConsts lc{~0ull, h->p.tol, KM_CONV_NONE, h->p.empty};
   cudaEvent_t ev[6];
   for (auto& x : ev) KM_CUDA_TRY(cudaEventCreate(&x));
+  // One iteration captured as a graph (the same kernels as the fit's graph)
+  // with event-record nodes between the stages; each replay is one iteration.
+  auto enqueue = [&](bool external) -> km_status {
+    const unsigned fl = external ? cudaEventRecordExternal : 0u;
+    km_status r = KM_OK;
+    cudaEventRecordWithFlags(ev[0], e.stream, fl);
+    r = e.enqueue_distance(nullptr);
+    cudaEventRecordWithFlags(ev[1], e.stream, fl);
+    if (r == KM_OK) r = e.enqueue_refine();
+    cudaEventRecordWithFlags(ev[2], e.stream, fl);
+    if (r == KM_OK) r = e.enqueue_sort(e.labels);
+    cudaEventRecordWithFlags(ev[3], e.stream, fl);
+    if (r == KM_OK) r = e.enqueue_update_step(h->p.tol);
+    cudaEventRecordWithFlags(ev[4], e.stream, fl);
+    if (r == KM_OK) r = e.enqueue_finalize(lc);
+    cudaEventRecordWithFlags(ev[5], e.stream, fl);
+    return r;
+  };
+  cudaGraphExec_t gx = nullptr;
+  {
+    cudaGraph_t g = nullptr;
+    km_status cs = KM_ERR_CUDA;
+    if (cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      cs = enqueue(true);
+      if (cudaStreamEndCapture(e.stream, &g) != cudaSuccess) cs = KM_ERR_CUDA;
+    }
+    if (cs == KM_OK && g && cudaGraphInstantiate(&gx, g, 0) != cudaSuccess) gx = nullptr;
+    if (g) cudaGraphDestroy(g);
+    (void)cudaGetLastError();   // no graph: the stages are launched directly below
+  }
   double acc[5] = {0, 0, 0, 0, 0};
   km_status rc = KM_OK;
   for (uint64_t it = 0; it < iters && rc == KM_OK; ++it) {
-    cudaEventRecord(ev[0], e.stream);
-    rc = e.enqueue_distance(nullptr);
-    cudaEventRecord(ev[1], e.stream);
-    if (rc == KM_OK) rc = e.enqueue_refine();
-    cudaEventRecord(ev[2], e.stream);
-    if (rc == KM_OK) rc = e.enqueue_sort(e.labels);
-    cudaEventRecord(ev[3], e.stream);
-    if (rc == KM_OK) rc = e.enqueue_update_step(h->p.tol);
-    cudaEventRecord(ev[4], e.stream);
-    if (rc == KM_OK) rc = e.enqueue_finalize(lc);
-    cudaEventRecord(ev[5], e.stream);
+    if (gx) {
+      if (cudaGraphLaunch(gx, e.stream) != cudaSuccess) { rc = KM_ERR_CUDA; break; }
+    } else {
+      rc = enqueue(false);
+    }
     if (cudaEventSynchronize(ev[5]) != cudaSuccess) { rc = KM_ERR_CUDA; break; }
     for (int s = 0; s < 5; ++s) {
       float ms = 0;
@@ -366,6 +390,7 @@ km_status km_lloyd_profile(km_lloyd* h, uint64_t iters, double* stage_ms) {
       acc[s] += ms;
     }
   }
+  if (gx) cudaGraphExecDestroy(gx);
   for (auto& x : ev) cudaEventDestroy(x);
   KM_TRY(rc);
   KM_TRY(e.check_device_error());

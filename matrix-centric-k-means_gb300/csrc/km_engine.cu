@@ -360,10 +360,7 @@ km_status LloydEngine::read_state() {
 
 km_status LloydEngine::check_device_error() {
   KM_TRY(read_state());
-  if (h_st->err & KM_DEVERR_TIMEOUT) return KM_ERR_TIMEOUT;
-  if (h_st->err & KM_DEVERR_NONFINITE) return KM_ERR_ARG;
-  if (h_st->err & KM_DEVERR_OVERFLOW) return KM_ERR_ARG;
-  return KM_OK;
+  return status_of_device_error(h_st->err);
 }
 
 }  // namespace km

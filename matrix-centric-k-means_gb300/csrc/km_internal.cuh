@@ -62,6 +62,13 @@ enum : uint32_t {
   KM_DEVERR_OVERFLOW = 4u   // refinement list overflow (cannot happen: list holds n)
 };
 
+// Host mapping of the device error bits to a status (timeouts first).
+inline km_status status_of_device_error(uint32_t err) {
+  if (err & KM_DEVERR_TIMEOUT) return KM_ERR_TIMEOUT;
+  if (err & (KM_DEVERR_NONFINITE | KM_DEVERR_OVERFLOW)) return KM_ERR_ARG;
+  return KM_OK;
+}
+
 // Per-fit constants passed by value to the kernels that end an iteration
 // (finalize_kernel, kkm_control_kernel).
 struct LoopConsts {

@@ -14,10 +14,15 @@
 // library holds its KM_NOALLOC_SCRATCH_BYTES until the process exits.  Host
 // code only ever sees a host-side stand-in for it, so the device address is
 // looked up with cudaGetSymbolAddress, once per device, with that device
-// current, on the first call made on that device.  Every call shares the
+// current, on the first call made on that device.  With lazy module loading
+// (the CUDA default) the array may only be placed on the device at that first
+// call, so make the first call before a host pool claims the device memory
+// (or load modules eagerly, CUDA_MODULE_LOADING=EAGER).  Every call shares the
 // array, which keeps the last call's contents: the loop state is cleared at the
 // start of each call, and calls that overlap on the GPU (two streams, two host
-// threads) race on it.
+// threads) race on it.  Each call ends with one synchronisation of its stream
+// (it reads the error bits back), so it cannot be recorded into a CUDA graph
+// by stream capture.
 #include "km_lloyd.cuh"
 
 #include <mutex>
@@ -109,13 +114,17 @@ extern "C" km_status km_update_noalloc(const float* X_dev, const uint32_t* label
   cluster_scan_kernel<<<1, 1024, 0, s>>>(counts, k, cstart, st, nullptr);
   seg_scatter_kernel<<<hb, wpb * 32, smem, s>>>(labels_dev, n, k, seg, nseg, seghist, cstart, perm, st);
   KM_CUDA_TRY(cudaGetLastError());
-  // Labels >= k are rejected before the sums run (the histogram flags them).
-  uint32_t err = 0;
-  KM_CUDA_TRY(cudaMemcpyAsync(&err, &st->err, sizeof(err), cudaMemcpyDeviceToHost, s));
-  KM_CUDA_TRY(cudaStreamSynchronize(s));
-  if (err) return KM_ERR_ARG;
+  // A label >= k only sets an error bit: the sort skips such rows, so every
+  // permutation slot the sums read was written by this call and the sums stay
+  // in bounds.  The status is read once, after all the work.
   KM_TRY(launch_update_sums(X_dev, perm, cstart, d, k, nullptr, C_dev, nullptr, nullptr, st, s));
   if (counts_dev)
     KM_CUDA_TRY(cudaMemcpyAsync(counts_dev, counts, sizeof(uint32_t) * k, cudaMemcpyDeviceToDevice, s));
-  return KM_OK;
+  // The one host synchronisation of the call: the error bits of the sort
+  // (labels >= k) and of the sums (a bounded wait that ran out).  The copy
+  // lands in `err` before the synchronisation returns.
+  uint32_t err = 0;
+  KM_CUDA_TRY(cudaMemcpyAsync(&err, &st->err, sizeof(err), cudaMemcpyDeviceToHost, s));
+  KM_CUDA_TRY(cudaStreamSynchronize(s));
+  return status_of_device_error(err);
 }

@@ -3,7 +3,11 @@
 # sources where they lie in the reference tree into oracle/_ref/, for use as a
 # checker of the oracle restatement (tests) and as the reference CPU baseline.
 #
-#   oracle/build_ref.sh [REFERENCE_ROOT]      (default: /root/reference)
+#   oracle/build_ref.sh [REFERENCE_ROOT]
+#   oracle/build_ref.sh --print-root          (prints the resolved root)
+#
+# The root is the argument, else $KM_REFERENCE_ROOT, else /root/reference;
+# nothing else in the repository names the reference tree's location.
 #
 # Only the reference's kmeans.cpp and its headers are compiled, together with
 # oracle/ref_shim.cpp (a C entry point); the reference's header-only dataset
@@ -15,7 +19,11 @@
 # x86-64 (no FMA without -march), and makes an aarch64 build agree with it.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+if [ "${1:-}" = "--print-root" ]; then
+  echo "${KM_REFERENCE_ROOT:-/root/reference}"
+  exit 0
+fi
+REF="${1:-${KM_REFERENCE_ROOT:-/root/reference}}"
 SRC="$REF/comparisons/CPU_Kmeans/src/kmeans.cpp"
 if [ ! -f "$SRC" ]; then
   echo "build_ref.sh: reference sources not found under $REF; skipping" >&2

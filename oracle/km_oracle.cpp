@@ -263,10 +263,15 @@ uint64_t orc_lloyd_f32(const float* X, uint64_t n, uint32_t d, uint32_t k, float
 // The same iteration in FP64 (distances, sums, scale and shift test in double,
 // lowest index on ties, empty cluster -> zero vector).  Initial centroids as
 // orc_lloyd_f32.  Used as the FP64 oracle for reduced-precision paths.
-uint64_t orc_lloyd_f64(const float* X, uint64_t n, uint32_t d, uint32_t k, double tol, int seed,
-                       uint64_t maxiter, const float* C0, int nthreads,
-                       uint32_t* labels_out, double* centroids_out, uint64_t* executed) {
+// objective_out (optional): the FP64 objective sum_i min_c ||x_i - c||^2 of the
+// last assignment step (against the centroids that step used).
+uint64_t orc_lloyd_f64_obj(const float* X, uint64_t n, uint32_t d, uint32_t k, double tol, int seed,
+                           uint64_t maxiter, const float* C0, int nthreads,
+                           uint32_t* labels_out, double* centroids_out, uint64_t* executed,
+                           double* objective_out) {
   if (n == 0 || d == 0 || k == 0 || k > n) return UINT64_MAX;
+  const int nt = std::max(1, nthreads);
+  std::vector<double> objpart(nt, 0.0);
   std::vector<double> C((uint64_t)k * d), Cprev, Ct((uint64_t)d * k);
   std::vector<uint32_t> labels(n), counts(k);
   if (C0) {
@@ -282,12 +287,16 @@ uint64_t orc_lloyd_f64(const float* X, uint64_t n, uint32_t d, uint32_t k, doubl
   while (iter++ < maxiter) {
     for (uint32_t c = 0; c < k; ++c)
       for (uint32_t j = 0; j < d; ++j) Ct[(uint64_t)j * k + c] = C[(uint64_t)c * d + j];
-    parallel_for(nthreads, n, [&](int, uint64_t b, uint64_t e) {
+    std::fill(objpart.begin(), objpart.end(), 0.0);
+    parallel_for(nthreads, n, [&](int t, uint64_t b, uint64_t e) {
       std::vector<double> dist(k);
+      double o = 0.0;
       for (uint64_t i = b; i < e; ++i) {
         row_dists_f64(X + i * d, Ct.data(), d, k, dist.data());
         labels[i] = argmin_strict(dist.data(), k);
+        o += dist[labels[i]];
       }
+      objpart[t] = o;
     });
     std::fill(counts.begin(), counts.end(), 0u);
     for (uint64_t i = 0; i < n; ++i) counts[labels[i]]++;
@@ -317,7 +326,19 @@ uint64_t orc_lloyd_f64(const float* X, uint64_t n, uint32_t d, uint32_t k, doubl
   if (executed) *executed = std::min(iter, maxiter);
   std::memcpy(labels_out, labels.data(), sizeof(uint32_t) * n);
   if (centroids_out) std::memcpy(centroids_out, C.data(), sizeof(double) * k * d);
+  if (objective_out) {
+    double o = 0.0;
+    for (double v : objpart) o += v;
+    *objective_out = o;
+  }
   return converged;
+}
+
+uint64_t orc_lloyd_f64(const float* X, uint64_t n, uint32_t d, uint32_t k, double tol, int seed,
+                       uint64_t maxiter, const float* C0, int nthreads,
+                       uint32_t* labels_out, double* centroids_out, uint64_t* executed) {
+  return orc_lloyd_f64_obj(X, n, d, k, tol, seed, maxiter, C0, nthreads, labels_out, centroids_out,
+                           executed, nullptr);
 }
 
 // FP64 k-means objective sum_i ||x_i - c_{label_i}||^2 for float centroids.

@@ -13,7 +13,21 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[1]
 PKG = ROOT / "matrix-centric-k-means_gb300"
 ORACLE = ROOT / "oracle"
-REFERENCE = Path("/root/reference")
+
+
+def _reference_root() -> Path:
+    """The reference tree's root as oracle/build_ref.sh resolves it (its
+    argument, $KM_REFERENCE_ROOT, or its default); it may not exist (the GPU
+    box has no reference tree)."""
+    try:
+        out = subprocess.run([str(ORACLE / "build_ref.sh"), "--print-root"], capture_output=True,
+                             text=True, check=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return Path("/nonexistent-reference-root")
+    return Path(out)
+
+
+REFERENCE = _reference_root()
 
 _km = None
 
@@ -54,6 +68,9 @@ def oracle():
         lib.orc_lloyd_f32.argtypes = [vp, u64, u32, u32, f32, i32, u64, vp, i32, vp, vp, C.POINTER(u64)]
         lib.orc_lloyd_f64.restype = u64
         lib.orc_lloyd_f64.argtypes = [vp, u64, u32, u32, C.c_double, i32, u64, vp, i32, vp, vp, C.POINTER(u64)]
+        lib.orc_lloyd_f64_obj.restype = u64
+        lib.orc_lloyd_f64_obj.argtypes = [vp, u64, u32, u32, C.c_double, i32, u64, vp, i32, vp, vp,
+                                          C.POINTER(u64), C.POINTER(C.c_double)]
         lib.orc_inertia.restype = C.c_double
         lib.orc_inertia.argtypes = [vp, vp, vp, u64, u32, u32, i32]
         lib.orc_kernel_matrix.restype = None
@@ -88,6 +105,22 @@ def orc_lloyd64(X, k, tol, seed, maxiter, C0=None, threads=8):
                                 None if c0 is None else c0.ctypes.data, threads, lab.ctypes.data,
                                 cen.ctypes.data, C.byref(ex))
     return int(it), lab, cen, int(ex.value)
+
+
+def orc_lloyd64_obj(X, k, tol, seed, maxiter, C0=None, threads=8):
+    """FP64 oracle Lloyd; also returns the FP64 objective of its last
+    assignment step (iters, labels, centroids, executed, objective)."""
+    X = np.ascontiguousarray(X, np.float32)
+    n, d = X.shape
+    lab = np.empty(n, np.uint32)
+    cen = np.empty((k, d), np.float64)
+    ex = C.c_uint64(0)
+    obj = C.c_double(0.0)
+    c0 = None if C0 is None else np.ascontiguousarray(C0, np.float32)
+    it = oracle().orc_lloyd_f64_obj(X.ctypes.data, n, d, k, tol, seed, maxiter,
+                                    None if c0 is None else c0.ctypes.data, threads, lab.ctypes.data,
+                                    cen.ctypes.data, C.byref(ex), C.byref(obj))
+    return int(it), lab, cen, int(ex.value), float(obj.value)
 
 
 def orc_assign(X, Cc, threads=8):
@@ -138,8 +171,7 @@ def reference_lib():
     if _ref is None:
         so = ORACLE / "_ref" / "libref_kmeans.so"
         if not so.exists() and REFERENCE.exists():
-            subprocess.run([str(ORACLE / "build_ref.sh"), str(REFERENCE)], check=True,
-                           capture_output=True)
+            subprocess.run([str(ORACLE / "build_ref.sh")], check=True, capture_output=True)
         if not so.exists():
             return None
         try:
@@ -172,8 +204,7 @@ def reference_io_lib():
     if _ref_io is None:
         so = ORACLE / "_ref" / "libref_io.so"
         if not so.exists() and REFERENCE.exists():
-            subprocess.run([str(ORACLE / "build_ref.sh"), str(REFERENCE)], check=True,
-                           capture_output=True)
+            subprocess.run([str(ORACLE / "build_ref.sh")], check=True, capture_output=True)
         if not so.exists():
             return None
         lib = C.CDLL(str(so))
@@ -272,6 +303,28 @@ def synth_blobs_np(n, d, blobs, lo, hi, sigma, seed, round_clip=False):
     if round_clip:
         v = np.minimum(hi, np.maximum(lo, np.rint(v))) + 0.0  # -0 -> +0
     return v.astype(np.float32), b.astype(np.uint32)
+
+
+def synth_blobs_np_chunked(n, d, blobs, lo, hi, sigma, seed, rows_per_chunk=65536):
+    """synth_blobs_np for large n, generated in row chunks (same values: every
+    draw is indexed by its global row and column)."""
+    k0, k1, k2 = (_stream_key(seed, s) for s in range(3))
+    center = (lo + (hi - lo) * _uniform(k0, np.arange(blobs * d, dtype=np.uint64))).reshape(blobs, d)
+    out = np.empty((n, d), np.float32)
+    lab = np.empty(n, np.uint32)
+    for r0 in range(0, n, rows_per_chunk):
+        r1 = min(n, r0 + rows_per_chunk)
+        b = (_uniform(k1, np.arange(r0, r1, dtype=np.uint64)) * blobs).astype(np.int64)
+        b = np.minimum(b, blobs - 1)
+        idx = np.arange(r0 * d, r1 * d, dtype=np.uint64) * np.uint64(4)
+        s = _uniform(k2, idx)
+        s = s + _uniform(k2, idx + np.uint64(1))
+        s = s + _uniform(k2, idx + np.uint64(2))
+        s = s + _uniform(k2, idx + np.uint64(3))
+        z = ((s - 2.0) * np.sqrt(3.0)).reshape(r1 - r0, d)
+        out[r0:r1] = (center[b] + sigma * z).astype(np.float32)
+        lab[r0:r1] = b
+    return out, lab
 
 
 def config1_data(seed=0):

@@ -28,7 +28,7 @@ def test_cli_lists_every_workload():
         assert w in out.stdout
 
 
-def test_reference_arm_line(km):
+def test_reference_arm_line():
     b = load_bench()
     args = argparse.Namespace(gpus=1, steps=1, warmup=0, impl="reference", workload="lloyd")
     line = b.reference_arm(args, 0)
@@ -44,6 +44,18 @@ def test_reference_arm_line(km):
                            "d2h_bytes_per_step": 0}
     assert line["config"]["workload"].startswith("lloyd n=1048576 d=128 k=256")
     assert b.reference_arm(args, 1) is None                   # other ranks do no work
+
+
+def test_reference_arm_loads_no_product_library():
+    """In a process of its own the reference arm maps only oracle libraries:
+    its data come from the numpy twin of the product's generator."""
+    out = subprocess.run([sys.executable, str(BENCH), "--impl", "reference", "--steps", "1", "--warmup", "0"],
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert not [x for x in line["repo_libraries_loaded"] if x.startswith("matrix-centric-k-means_gb300")]
+    assert any(x.startswith("oracle") for x in line["repo_libraries_loaded"])
 
 
 @pytest.mark.parametrize("use_ref", [False, True])
