@@ -163,3 +163,31 @@ def test_kernel_kmeans_oracle_vs_numpy(kind, params):
     assert it == it_np
     np.testing.assert_array_equal(lab, lab_np)
     assert abs(sc.value - sc_np) <= 1e-9 * max(1.0, abs(sc_np))
+
+
+@pytest.mark.parametrize("kind,params", [(1, (1 / 16, 1, 2, 1)), (3, (1, 0, 1, 0.7)), (0, (1, 0, 1, 1))])
+def test_kkm_step_blocked_matches_oracle_iteration(kind, params):
+    """oracle/kkm_step.py (K formed block by block, for n too large for an n x n
+    FP64 matrix) gives the labels and score of one iteration of the oracle's
+    orc_kernel_kmeans from the same labels, including an emptied cluster."""
+    import ctypes as C
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("kkm_step", helpers.ORACLE / "kkm_step.py")
+    ks = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(ks)
+    gamma, coef, degree, sigma = params
+    X, _ = helpers.synth_blobs_np(700, 16, 6, -1, 1, 0.3, 8)
+    n, d = X.shape
+    k = 7
+    K = np.empty((n, n))
+    helpers.oracle().orc_kernel_matrix(X.ctypes.data, n, d, kind, gamma, coef, degree, sigma, 4, K.ctypes.data)
+    lab0 = np.random.default_rng(3).integers(0, k - 1, n).astype(np.uint32)     # cluster k-1 empty
+    lab = lab0.copy()
+    sc = C.c_double(0)
+    ex = C.c_uint64(0)
+    helpers.oracle().orc_kernel_kmeans(K.ctypes.data, n, k, 1, 0.0, 0, 4, lab.ctypes.data, C.byref(sc), C.byref(ex))
+    new, score = ks.kkm_step_f64(X, lab0, k, kind, gamma, coef, degree, sigma, block=128, workers=3)
+    np.testing.assert_array_equal(new, lab)
+    assert abs(score - sc.value) <= 1e-9 * max(1.0, abs(sc.value))
+    diag = ks.kernel_diag(X, kind, gamma, coef, degree, sigma)
+    np.testing.assert_allclose(diag, np.diagonal(K), rtol=1e-12, atol=1e-12)
