@@ -424,17 +424,18 @@ def stages_only(args):
     import torch
     import helpers
     km = helpers.km()
-    X = make_data(km)
+    n = args.rows or N
+    X = make_data(km)[:n]
     Xd = torch.from_numpy(X).cuda()
     stream = torch.cuda.Stream()
     names = ["distance+argmin", "refine", "label sort", "centroid sums", "finalize+control"]
     with torch.cuda.stream(stream):
-        m = km.Lloyd(N, D, K, tol=TOL, seed=KM_SEED, maxiter=5, precision=args.precision, conv="none",
+        m = km.Lloyd(n, D, K, tol=TOL, seed=KM_SEED, maxiter=5, precision=args.precision, conv="none",
                      stream=stream.cuda_stream).set_data(Xd)
         m.fit(want_centroids=False)
         st = m.profile(10)
         m.close()
-    return {"workload": bench_config(1)["workload"], "precision": args.precision,
+    return {"workload": bench_config(1)["workload"], "rows": n, "precision": args.precision,
             "stages_ms": dict(zip(names, st))}
 
 
@@ -808,7 +809,8 @@ def main():
                     help="lloyd only: a 5-iteration fit and the per-stage timer (Lloyd.profile) of "
                          "--precision, printed as one JSON line (a short command for profilers)")
     ap.add_argument("--rows", type=int, default=0,
-                    help="bigk only: fewer rows than the workload's n (a smaller case for profilers)")
+                    help="bigk and --stages-only: the first ROWS points of the workload instead of all n "
+                         "(a smaller case for profilers)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = (200 if (args.workload == "lloyd" and args.impl == "ours")

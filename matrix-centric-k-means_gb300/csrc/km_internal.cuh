@@ -207,14 +207,25 @@ __device__ __forceinline__ void seg_push(T* q, uint32_t* cnt, uint64_t seg, bool
 // Candidate threshold for one row: every centroid with fast value v(c) > tau
 // has a reference CPU distance strictly above the row's best (the TieBound
 // argument with E1 <= Emax), so the reference argmin lies in {c : v(c) <= tau}.
-__device__ __forceinline__ float tie_tau(float X2, float v1, float cmax, const TieBound& tb) {
+// The row-dependent part of tie_tau (T = bound of ||x||^2, Em = the largest
+// fast-path error), so that tau can be evaluated for several v1 of one row.
+struct TauRow {
+  float T, Em;
+};
+__device__ __forceinline__ TauRow tie_tau_row(float X2, float cmax, const TieBound& tb) {
   const float nx = sqrtf(X2) * 1.0000005f;
-  const float T = X2 * 1.0000003f;
-  const float Em = tb.A * nx * cmax + tb.B * cmax * cmax;
-  const float s = fmaxf(0.0f, 2.0f * T + v1 + 2.0f * Em);
+  return TauRow{X2 * 1.0000003f, tb.A * nx * cmax + tb.B * cmax * cmax};
+}
+// Non-decreasing in v1 (every operation is monotone), so a threshold taken at
+// a running minimum is never below the one of the final minimum.
+__device__ __forceinline__ float tie_tau_at(const TauRow& r, float v1, const TieBound& tb) {
+  const float s = fmaxf(0.0f, 2.0f * r.T + v1 + 2.0f * r.Em);
   const float sg = tb.safety * tb.g;
-  float tau = (v1 + tb.safety * (2.0f * Em + tb.g * s) + 1e-30f) / (1.0f - sg);
+  float tau = (v1 + tb.safety * (2.0f * r.Em + tb.g * s) + 1e-30f) / (1.0f - sg);
   return fmaxf(tau, v1);
+}
+__device__ __forceinline__ float tie_tau(float X2, float v1, float cmax, const TieBound& tb) {
+  return tie_tau_at(tie_tau_row(X2, cmax, tb), v1, tb);
 }
 
 // Reference CPU distance, bit-exact: float, j ascending, no contraction.

@@ -44,23 +44,48 @@ namespace km {
 
 namespace {
 
-constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_SETS = 3;                            // k <= 256 kernel: epilogue sets of four warps
+constexpr int TC_EPI_WARPS = 4 * TC_SETS;
 constexpr int TC_THREADS = 32 * (4 + TC_EPI_WARPS);
+constexpr int TCC_THREADS = 32 * (4 + 8);               // chunked kernel: two sets of four
 constexpr int TC_M = 128;
 constexpr uint64_t WAIT_NS = 2000000000ull;
 constexpr uint32_t A_UNIT = TC_M * 128;  // bytes of one 128-row x 64-col BF16 K-block
+constexpr uint32_t TC_MAX_UNITS = 16;
+// Suspend-time hint of the k <= 256 kernel's waits: a waiting warp sleeps
+// (until the phase completes) instead of spinning on issue slots the epilogue needs.
+constexpr uint32_t TC_HINT_NS = 1000;
+// Accumulator-full barriers: tile t (this CTA's t-th) completes tfull[t % TC_NTF].
+// Each of them is waited on by one epilogue set only (set t % TC_SETS), tile
+// after tile, so a parity wait never aliases another set's phase.
+constexpr int TC_NTF = 2 * TC_SETS;
 
 struct TcSmem {
-  uint64_t full[16];
-  uint64_t empty[16];
+  uint64_t full[TC_MAX_UNITS];
+  uint64_t empty[TC_MAX_UNITS];
   uint64_t bfull;
-  uint64_t tfull[2];
+  uint64_t tfull[TC_NTF];
   uint64_t tempty[2];
   uint64_t tdone;
-  uint64_t pairbar[4];      // epilogue: the two warps of TMEM lane quadrant q
   uint32_t tmem_base;
   int abort;
 };
+
+// Centroid norms as the epilogue reads them: padded with +inf to 256.
+struct TcXch {
+  float cn2[256];
+};
+
+__device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
 
 template <int MODE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -72,6 +97,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
                  RefineQueues rq, float* __restrict__ Dout) {
   constexpr bool ALO = MODE == TC_SPLIT3;      // point operand has a lo part
   constexpr bool BLO = MODE != TC_PLAIN;       // centroid operand has a lo part
+  constexpr uint32_t UPK = ALO ? 2u : 1u;      // ring units per K block (hi, then lo)
   if (st->done) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -79,22 +105,29 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   const uint32_t b_bytes = KB * kp * 128u;              // one of hi / lo
   uint8_t* sB = smem;
   uint8_t* sA = smem + b_bytes * (BLO ? 2u : 1u);
-  const uint32_t unit_bytes = A_UNIT * (ALO ? 2u : 1u);
-  float* xch = reinterpret_cast<float*>(sA + (size_t)S * unit_bytes);   // [2][TC_M] row exchange
-  TcSmem* ts = reinterpret_cast<TcSmem*>(xch + 2 * TC_M);
+  TcXch* xch = reinterpret_cast<TcXch*>(sA + (size_t)S * A_UNIT);
+  TcSmem* ts = reinterpret_cast<TcSmem*>(xch + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t ntiles = (n + TC_M - 1) / TC_M;
   const float cmax = st->cmax;
+  const float finf = __int_as_float(0x7f800000);
 
   if (threadIdx.x == 0) {
     for (uint32_t s = 0; s < S; ++s) { mbar_init(&ts->full[s], 1); mbar_init(&ts->empty[s], 1); }
     mbar_init(&ts->bfull, 1);
-    for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], TC_EPI_WARPS); }
+    for (int b = 0; b < TC_NTF; ++b) mbar_init(&ts->tfull[b], 1);
+    for (int b = 0; b < 2; ++b) mbar_init(&ts->tempty[b], 4);
     mbar_init(&ts->tdone, 1);
-    for (int qq = 0; qq < 4; ++qq) mbar_init(&ts->pairbar[qq], 2);
     ts->abort = 0;
     mbar_fence_init();
+  }
+  if (warp >= 4) {
+    // centroid norms (padded with +inf by the host to a multiple of 64) into
+    // shared memory, +inf up to 256
+    const uint32_t kp64 = (kp + 63u) & ~63u;
+    for (uint32_t i = threadIdx.x - 128u; i < 256u; i += 32u * TC_EPI_WARPS)
+      xch->cn2[i] = i < kp64 ? cn2[i] : finf;
   }
   if (warp == 2) tmem_alloc(&ts->tmem_base, 2u * nalloc);
   tc_fence_before();
@@ -119,16 +152,22 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
         tma_load_2d(sB + (size_t)kb * kp * 128u, &tmB, (int)(kb * 64), 0, &ts->bfull);
         if (BLO) tma_load_2d(sB + b_bytes + (size_t)kb * kp * 128u, &tmBlo, (int)(kb * 64), 0, &ts->bfull);
       }
+      // Ring of S units of one 128 x 64 BF16 block each: per K block the hi
+      // part, then (split form) the lo part.
       uint64_t u = 0;
       bool ok = true;
       for (uint64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        for (uint32_t kb = 0; kb < KB; ++kb, ++u) {
-          const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
-          if (!mbar_wait_bounded(&ts->empty[s], ph ^ 1u, abort_flag, WAIT_NS)) { fail(1); ok = false; break; }
-          mbar_arrive_expect_tx(&ts->full[s], unit_bytes);
-          uint8_t* dst = sA + (size_t)s * unit_bytes;
-          tma_load_2d(dst, &tmA, (int)(kb * 64), (int)(tile * TC_M), &ts->full[s]);
-          if (ALO) tma_load_2d(dst + A_UNIT, &tmAlo, (int)(kb * 64), (int)(tile * TC_M), &ts->full[s]);
+        for (uint32_t kb = 0; kb < KB && ok; ++kb) {
+#pragma unroll
+          for (uint32_t part = 0; part < UPK; ++part, ++u) {
+            const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
+            if (!mbar_wait_bounded(&ts->empty[s], ph ^ 1u, abort_flag, WAIT_NS, TC_HINT_NS)) {
+              fail(1); ok = false; break;
+            }
+            mbar_arrive_expect_tx(&ts->full[s], A_UNIT);
+            tma_load_2d(sA + (size_t)s * A_UNIT, part ? &tmAlo : &tmA, (int)(kb * 64), (int)(tile * TC_M),
+                        &ts->full[s]);
+          }
         }
       }
       // Drain: every issued copy must land before the CTA exits (these waits
@@ -152,14 +191,20 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       bool issued = false;
       for (uint64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++t) {
         const uint32_t buf = (uint32_t)(t & 1u), use = (uint32_t)(t >> 1);
-        if (!mbar_wait_bounded(&ts->tempty[buf], (use & 1u) ^ 1u, abort_flag, WAIT_NS)) { fail(3); ok = false; break; }
+        if (!mbar_wait_bounded(&ts->tempty[buf], (use & 1u) ^ 1u, abort_flag, WAIT_NS, TC_HINT_NS)) {
+          fail(3); ok = false; break;
+        }
         tc_fence_after();
         const uint32_t dt = tmem_base + buf * nalloc;
-        for (uint32_t kb = 0; kb < KB; ++kb, ++u) {
-          const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
-          if (!mbar_wait_bounded(&ts->full[s], ph, abort_flag, WAIT_NS)) { fail(4); ok = false; break; }
+        for (uint32_t kb = 0; kb < KB; ++kb, u += UPK) {
+          const uint32_t sh = (uint32_t)(u % S), phh = (uint32_t)((u / S) & 1u);
+          const uint32_t sl = (uint32_t)((u + 1) % S), phl = (uint32_t)(((u + 1) / S) & 1u);
+          if (!mbar_wait_bounded(&ts->full[sh], phh, abort_flag, WAIT_NS, TC_HINT_NS) ||
+              (ALO && !mbar_wait_bounded(&ts->full[sl], phl, abort_flag, WAIT_NS, TC_HINT_NS))) {
+            fail(4); ok = false; break;
+          }
           tc_fence_after();
-          const uint32_t a0 = sA0 + s * unit_bytes;
+          const uint32_t a0 = sA0 + sh * A_UNIT, al = sA0 + sl * A_UNIT;
           const uint32_t b0 = sB0 + kb * kp * 128u;
 #pragma unroll
           for (uint32_t kk = 0; kk < 4; ++kk) {
@@ -167,13 +212,14 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
             const uint64_t bd = smem_desc_sw128(b0 + kk * 32u);
             tc_mma_bf16(dt, ad, bd, idesc, (kb | kk) != 0u ? 1u : 0u);
             if (BLO) tc_mma_bf16(dt, ad, smem_desc_sw128(b0 + b_bytes + kk * 32u), idesc, 1u);
-            if (ALO) tc_mma_bf16(dt, smem_desc_sw128(a0 + A_UNIT + kk * 32u), bd, idesc, 1u);
+            if (ALO) tc_mma_bf16(dt, smem_desc_sw128(al + kk * 32u), bd, idesc, 1u);
           }
-          tc_commit(&ts->empty[s]);
+          tc_commit(&ts->empty[sh]);
+          if (ALO) tc_commit(&ts->empty[sl]);
           issued = true;
         }
         if (!ok) break;
-        tc_commit(&ts->tfull[buf]);
+        tc_commit(&ts->tfull[t % TC_NTF]);
       }
       // All MMAs of this thread complete before teardown.
       if (issued) {
@@ -183,146 +229,130 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       }
     }
   } else if (warp >= 4) {
-    // Epilogue: the eight warps take every tile of this CTA together.  Warp w
-    // owns TMEM lanes (rows) 32*(w%4)..+31 and half h = (w-4)/4 of the 64-column
-    // loads (h = 0 the lower columns), so a tile's accumulator is released after
-    // half the column work of one warp.  The two warps of a quadrant exchange the
-    // row's partial minimum, then the upper half's candidate summary, through
-    // xch and their pair mbarrier (two phases per tile, bounded waits).
-    const int q = warp & 3, h = (warp - 4) >> 2;
-    const uint32_t npair = (kp + 63) / 64;          // 64-column loads in all
-    const uint32_t nlo = (npair + 1) / 2;           // of which half 0 takes the first nlo
-    const uint32_t pr0 = h ? nlo : 0u, pr1 = h ? npair : nlo;
+    // Epilogue: TC_SETS sets of four warps; set s takes this CTA's tiles
+    // t = s, s + TC_SETS, ... (TMEM buffer t % 2), so several tiles are in the
+    // epilogue at once and no warp waits for another.  Warp w of a set owns
+    // TMEM lanes (rows) 32*(w%4)..+31 and each thread sweeps its whole row in
+    // groups of 64 columns: v = ||c||^2 - 2 acc, the group minimum, the running
+    // minimum m, and the group's candidate mask {c < k : v(c) <= tau(m)}
+    // (tie_tau).  tau only grows with m, so each mask is a superset of the
+    // group's part of the final set {c : v(c) <= tau(v1)}, and a group whose
+    // minimum is above tau(v1) holds none of it.  The buffer is released after
+    // the last group's load.  Final candidates: the masks of the groups whose
+    // minimum is <= tau(v1); extra entries can only be centroids with
+    // v(c) > tau(v1), which the exact re-score never picks.
+    const int q = warp & 3, set = (warp - 4) >> 2;
     const uint32_t r = (uint32_t)q * 32u + (uint32_t)lane;
-    uint64_t* pb = &ts->pairbar[q];
-    uint32_t pbuse = 0;                             // completed phases of pb
-    auto pair_sync = [&]() -> bool {
-      __syncwarp();
-      if (lane == 0) mbar_arrive(pb);
-      const bool ok = mbar_wait_bounded(pb, pbuse & 1u, abort_flag, WAIT_NS);
-      ++pbuse;
-      return __all_sync(0xffffffffu, ok);
-    };
-    uint64_t t = 0;
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
-      const uint32_t buf = (uint32_t)(t & 1u), use = (uint32_t)(t >> 1);
+    const uint32_t ng = (kp + 63u) / 64u;                // 64-column groups (1..4)
+    const float* cns = xch->cn2;
+    for (uint64_t t = (uint64_t)set;; t += TC_SETS) {
+      const uint64_t tile = blockIdx.x + t * gridDim.x;
+      if (tile >= ntiles) break;
+      const uint32_t buf = (uint32_t)(t & 1u);
       const uint64_t row = tile * TC_M + r;
-      const float x2 = (row < n) ? xn2[row] : 0.0f;
-      const bool okw = mbar_wait_bounded(&ts->tfull[buf], use & 1u, abort_flag, WAIT_NS);
+      const bool valid = row < n;
+      const float x2 = valid ? xn2[row] : 0.0f;
+      const TauRow tr = tie_tau_row(x2, cmax, tb);
+      const bool okw = mbar_wait_bounded(&ts->tfull[t % TC_NTF], (uint32_t)((t / TC_NTF) & 1u), abort_flag,
+                                         WAIT_NS, TC_HINT_NS);
       if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(5); break; }
       tc_fence_after();
-      const uint32_t tbase = tmem_base + (((uint32_t)q * 32u) << 16) + buf * nalloc;
-      // ---- pass 1: partial row minimum of v = ||c||^2 - 2 acc over this half ----
-      // eight independent min chains (four steps per 64 columns each)
-      float mv[8];
+      const uint32_t tb0 = tmem_base + (((uint32_t)q * 32u) << 16) + buf * nalloc;
+      float m = finf;
+      float gmin[4];
+      uint32_t glo[4], ghi[4];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) mv[i] = __int_as_float(0x7f800000);
-      for (uint32_t pr = pr0; pr < pr1; ++pr) {
+      for (uint32_t g = 0; g < 4; ++g) {
+        gmin[g] = finf; glo[g] = 0u; ghi[g] = 0u;
+        if (g >= ng) continue;
+        const uint32_t cg = g * 64u;
+        const uint32_t nld = min(4u, (kp - cg) / 16u);   // 16-column loads in this group
+        // acc holds the accumulator, then (in place) v = ||c||^2 - 2 acc
         uint32_t acc[64];
-        tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
-        tmem_ld_wait();
-        const float4* cn4 = reinterpret_cast<const float4*>(cn2 + pr * 64u);
+        if (nld == 4u) {
+          tmem_ld_32x32b_x64(tb0 + cg, acc);
+        } else {
 #pragma unroll
-        for (int j4 = 0; j4 < 16; ++j4) {
-          const float4 cc = __ldg(cn4 + j4);
-          const float2 va = dist_pair(acc[4 * j4 + 0], acc[4 * j4 + 1], cc.x, cc.y);
-          const float2 vb = dist_pair(acc[4 * j4 + 2], acc[4 * j4 + 3], cc.z, cc.w);
-          mv[(2 * j4) & 7] = fmin3(mv[(2 * j4) & 7], va.x, va.y);
-          mv[(2 * j4 + 1) & 7] = fmin3(mv[(2 * j4 + 1) & 7], vb.x, vb.y);
+          for (uint32_t u = 0; u < 4; ++u) {
+            if (u < nld) {
+              tmem_ld_32x32b_x16(tb0 + cg + u * 16u, acc + 16u * u);
+            } else {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) acc[16u * u + j] = 0u;  // v = +inf from the padded norms
+            }
+          }
         }
-      }
-      const float mh = fminf(fmin3(mv[0], mv[1], mv[2]), fmin3(mv[3], mv[4], fmin3(mv[5], mv[6], mv[7])));
-      xch[h * TC_M + r] = mh;
-      if (!pair_sync()) { if (lane == 0) fail(6); break; }
-      const float v1 = fminf(mh, xch[(1 - h) * TC_M + r]);
-      const float tau = tie_tau(x2, v1, cmax, tb);
-      // ---- pass 2: this half's candidates {c < k : v(c) <= tau} in ascending order ----
-      uint32_t cnt = 0, got = 0, k0 = 0, k1 = 0, k2 = 0, k3 = 0;
-      bool released = false;
-      for (uint32_t pr = pr0; pr < pr1; ++pr) {
-        uint32_t acc[64];
-        tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
         tmem_ld_wait();
-        if (pr + 1 == pr1) {
-          // the last load of this tile has landed: the accumulator is free
+        if (g + 1u == ng) {
+          // last load of this tile: the accumulator buffer is free
           tc_fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&ts->tempty[buf]);
-          released = true;
         }
-        const float4* cn4 = reinterpret_cast<const float4*>(cn2 + pr * 64u);
-        uint32_t mm[2];
+        {
+          float m0 = finf, m1 = finf, m2 = finf, m3 = finf;
 #pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {
-          // four independent partial masks, one per column residue mod 4
-          uint32_t q0 = 0u, q1 = 0u, q2 = 0u, q3 = 0u;
-#pragma unroll
-          for (int j4 = 0; j4 < 8; ++j4) {
-            const float4 cc = __ldg(cn4 + 8 * hh + j4);
-            const int a = 32 * hh + 4 * j4;
-            const float2 va = dist_pair(acc[a + 0], acc[a + 1], cc.x, cc.y);
-            const float2 vb = dist_pair(acc[a + 2], acc[a + 3], cc.z, cc.w);
-            q0 |= (va.x <= tau ? 1u : 0u) << (4 * j4 + 0);
-            q1 |= (va.y <= tau ? 1u : 0u) << (4 * j4 + 1);
-            q2 |= (vb.x <= tau ? 1u : 0u) << (4 * j4 + 2);
-            q3 |= (vb.y <= tau ? 1u : 0u) << (4 * j4 + 3);
+          for (int j4 = 0; j4 < 16; ++j4) {
+            const float4 cc = *reinterpret_cast<const float4*>(cns + cg + 4 * j4);
+            const float2 va = dist_pair(acc[4 * j4 + 0], acc[4 * j4 + 1], cc.x, cc.y);
+            const float2 vb = dist_pair(acc[4 * j4 + 2], acc[4 * j4 + 3], cc.z, cc.w);
+            acc[4 * j4 + 0] = __float_as_uint(va.x); acc[4 * j4 + 1] = __float_as_uint(va.y);
+            acc[4 * j4 + 2] = __float_as_uint(vb.x); acc[4 * j4 + 3] = __float_as_uint(vb.y);
+            if (j4 & 1) { m2 = fmin3(m2, va.x, va.y); m3 = fmin3(m3, vb.x, vb.y); }
+            else        { m0 = fmin3(m0, va.x, va.y); m1 = fmin3(m1, vb.x, vb.y); }
           }
-          mm[hh] = (q0 | q1) | (q2 | q3);
+          gmin[g] = fminf(fminf(m0, m1), fminf(m2, m3));
         }
+        m = fminf(m, gmin[g]);
+        const float tau = tie_tau_at(tr, m, tb);
+        const uint32_t nval = cg < k ? min(64u, k - cg) : 0u;   // columns < k of this group
+        uint32_t p0 = 0u, p1 = 0u, p2 = 0u, p3 = 0u;
 #pragma unroll
-        for (int hh = 0; hh < 2; ++hh) {
-          const uint32_t c0 = pr * 64u + (uint32_t)hh * 32u;
-          uint32_t m = mm[hh] & ((c0 >= k) ? 0u : (k - c0 >= 32u ? 0xffffffffu : ((1u << (k - c0)) - 1u)));
-          cnt += (uint32_t)__popc(m);
-          while (m != 0u && got < 4u) {
-            const uint32_t col = c0 + (uint32_t)(__ffs(m) - 1);
-            m &= m - 1u;
-            k0 = (got == 0) ? col : k0; k1 = (got == 1) ? col : k1;
-            k2 = (got == 2) ? col : k2; k3 = (got == 3) ? col : k3;
-            ++got;
-          }
+        for (int j = 0; j < 32; j += 4) {
+          p0 |= (__uint_as_float(acc[j + 0]) <= tau ? 1u : 0u) << (j + 0);
+          p1 |= (__uint_as_float(acc[j + 1]) <= tau ? 1u : 0u) << (j + 1);
+          p2 |= (__uint_as_float(acc[j + 2]) <= tau ? 1u : 0u) << (j + 2);
+          p3 |= (__uint_as_float(acc[j + 3]) <= tau ? 1u : 0u) << (j + 3);
         }
-        if (Dout && row < n) {
+        glo[g] = ((p0 | p1) | (p2 | p3)) & (nval >= 32u ? 0xffffffffu : ((1u << nval) - 1u));
+        p0 = p1 = p2 = p3 = 0u;
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
+          p0 |= (__uint_as_float(acc[32 + j + 0]) <= tau ? 1u : 0u) << (j + 0);
+          p1 |= (__uint_as_float(acc[32 + j + 1]) <= tau ? 1u : 0u) << (j + 1);
+          p2 |= (__uint_as_float(acc[32 + j + 2]) <= tau ? 1u : 0u) << (j + 2);
+          p3 |= (__uint_as_float(acc[32 + j + 3]) <= tau ? 1u : 0u) << (j + 3);
+        }
+        ghi[g] = ((p0 | p1) | (p2 | p3)) &
+                 (nval >= 64u ? 0xffffffffu : (nval > 32u ? ((1u << (nval - 32u)) - 1u) : 0u));
+        if (Dout && valid) {
+#pragma unroll
           for (int j = 0; j < 64; ++j)
-            if (pr * 64u + j < k)
-              Dout[row * k + pr * 64u + j] = fmaf(-2.0f, __uint_as_float(acc[j]), __ldg(cn2 + pr * 64u + j)) + x2;
+            if ((uint32_t)j < nval) Dout[row * k + cg + j] = __uint_as_float(acc[j]) + x2;
         }
       }
-      if (!released) {                                   // this half had no columns
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&ts->tempty[buf]);
-      }
-      // The upper half hands its summary to the lower half: min(cnt, 7) and up
-      // to four column offsets (7 bits each, relative to the half's first
-      // column), written to the lower half's exchange slot, which only the
-      // upper half reads and has already read.
-      const uint32_t hbase = nlo * 64u;
-      if (h == 1) {
-        const uint32_t info = min(cnt, 7u) | (((k0 - hbase) & 127u) << 3) | (((k1 - hbase) & 127u) << 10) |
-                              (((k2 - hbase) & 127u) << 17) | (((k3 - hbase) & 127u) << 24);
-        xch[r] = __uint_as_float(info);
-      }
-      if (!pair_sync()) { if (lane == 0) fail(7); break; }
-      if (h == 1) continue;
-      {
-        const uint32_t info = __float_as_uint(xch[r]);
-        const uint32_t cb = info & 7u;
-        // merge: the lower half's candidates come first (lower columns)
+      // Final set: the masks of the groups whose minimum is within tau(v1),
+      // in column order; k0 is the lowest candidate index.  NaN anywhere
+      // (tau or v1) leaves cnt == 0: such a row takes the full path.
+      const float v1 = m;
+      const float tau = tie_tau_at(tr, v1, tb);
+      uint32_t cnt = 0, got = 0, k0 = 0, k1 = 0, k2 = 0, k3 = 0;
 #pragma unroll
-        for (uint32_t i = 0; i < 4; ++i) {
-          if (i < cb && got < 4u) {
-            const uint32_t col = hbase + ((info >> (3 + 7 * i)) & 127u);
+      for (uint32_t g = 0; g < 4; ++g) {
+        if (!(gmin[g] <= tau)) continue;
+        cnt += (uint32_t)(__popc(glo[g]) + __popc(ghi[g]));
+#pragma unroll
+        for (uint32_t hh = 0; hh < 2; ++hh) {
+          uint32_t mk = hh ? ghi[g] : glo[g];
+          while (mk != 0u && got < 4u) {
+            const uint32_t col = g * 64u + hh * 32u + (uint32_t)(__ffs(mk) - 1);
+            mk &= mk - 1u;
             k0 = (got == 0) ? col : k0; k1 = (got == 1) ? col : k1;
             k2 = (got == 2) ? col : k2; k3 = (got == 3) ? col : k3;
             ++got;
           }
         }
-        cnt += cb;
       }
-      // Candidates in ascending column order: k0 is the lowest index.  NaN
-      // anywhere (tau or v1) leaves cnt == 0: such a row takes the full path.
-      const bool valid = row < n;
       if (valid) {
         labels[row] = k0;
         if (mindist) mindist[row] = v1 + x2;
@@ -379,7 +409,7 @@ struct TcSmemC {
 __host__ __device__ constexpr uint32_t tcc_state_bytes(uint32_t T) { return T * TC_M * 8u; }
 
 template <int MODE>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(TCC_THREADS, 1)
 assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
                          const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo,
                          const float* __restrict__ cn2, const float* __restrict__ xn2, uint64_t n,
@@ -700,16 +730,16 @@ TcPlan plan_tc(uint32_t dp, uint32_t kp, int mode, uint64_t n, int num_sms) {
   if (dp == 0 || dp % 64 != 0 || kp < 16 || kp > 256 || kp % 16 != 0) return p;
   p.KB = dp / 64;
   const size_t b_bytes = (size_t)p.KB * kp * 128 * (mode != TC_PLAIN ? 2 : 1);
-  const size_t unit = (size_t)A_UNIT * (mode == TC_SPLIT3 ? 2 : 1);
-  const size_t fixed = 1024 /*align*/ + 2 * TC_M * sizeof(float) /*xch*/ + sizeof(TcSmem) + 64;
+  const size_t upk = mode == TC_SPLIT3 ? 2 : 1;             // ring units per K block
+  const size_t fixed = 1024 /*align*/ + sizeof(TcXch) + sizeof(TcSmem) + 64;
   const size_t budget = 227 * 1024;
-  if (b_bytes + fixed + 2 * unit > budget) return p;
-  size_t s = (budget - b_bytes - fixed) / unit;
-  if (s > 8) s = 8;
+  if (b_bytes + fixed + 2 * upk * A_UNIT > budget) return p;
+  size_t s = (budget - b_bytes - fixed) / A_UNIT;
+  if (s > TC_MAX_UNITS) s = TC_MAX_UNITS;
   p.stages = (uint32_t)s;
   p.nalloc = 64;                 // >= 64: a 64-column TMEM load never leaves the buffer
   while (p.nalloc < kp) p.nalloc <<= 1;
-  p.smem = b_bytes + fixed + s * unit;
+  p.smem = b_bytes + fixed + s * A_UNIT;
   const uint64_t ntiles = (n + TC_M - 1) / TC_M;
   p.grid = (int)std::min<uint64_t>(ntiles, (uint64_t)num_sms);
   if (p.grid < 1) p.grid = 1;
@@ -792,7 +822,7 @@ void launch_mode(const TcPlan& pl, const CUtensorMap& tmA, const CUtensorMap& tm
                  uint32_t kp, TieBound tb, DevState* st, uint32_t* labels, float* mindist,
                  const RefineQueues& rq, float* Dout, cudaStream_t s) {
   if (pl.chunked)
-    assign_tc_chunked_kernel<MODE><<<pl.grid, TC_THREADS, pl.smem, s>>>(
+    assign_tc_chunked_kernel<MODE><<<pl.grid, TCC_THREADS, pl.smem, s>>>(
         tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.NC, pl.KB, pl.stages, pl.T, tb, st, labels,
         mindist, rq, Dout);
   else
