@@ -341,6 +341,100 @@ uint64_t orc_lloyd_f64(const float* X, uint64_t n, uint32_t d, uint32_t k, doubl
                            executed, nullptr);
 }
 
+// Seeded greedy k-means++ as the product's device initialisation draws it:
+// the reference algorithm (src/kmeans.cu:447-769: first centroid uniform,
+// then per round s = 2 + ceil(ln k) candidates drawn with probability
+// proportional to the squared distance to the chosen set, raft::random::discrete
+// over min_distances :585-588; the candidate with the lowest total cost
+// sum_i min(d2_i, ||x_i - cand||^2) is kept, lowest index on equal cost,
+// :681-715; d2 updated with its distances, :721-724), with the draws taken
+// from std::mt19937_64(seed) instead of std::random_device: the first index
+// by uniform_int_distribution<uint64_t>(0, n-1), then (k-1)*s uniforms in
+// [0, 1), candidate j of round r using uniform (r-1)*s + j.  A draw u picks the
+// first row (ascending, rows with d2 > 0 only) whose FP64 prefix sum of d2
+// exceeds u * sum(d2); when every d2 is 0 the pick is floor(u * n).  Squared
+// distances are FP32 in the order of the device's warp reduction (per lane l
+// an fma chain over columns l, l+32, ..., then a butterfly over 16, 8, 4, 2, 1);
+// sums over rows are FP64.  picks receives the k row indices.  Returns 1 when
+// s exceeds 16 (the device's limit), else 0.
+namespace {
+inline float pp_dist32(const float* x, const float* c, uint32_t d) {
+  float p[32];
+  for (uint32_t l = 0; l < 32; ++l) {
+    float a = 0.0f;
+    for (uint32_t j = l; j < d; j += 32) {
+      const float u = x[j] - c[j];
+      a = std::fma(u, u, a);
+    }
+    p[l] = a;
+  }
+  for (uint32_t o = 16; o > 0; o >>= 1) {
+    float q[32];
+    for (uint32_t l = 0; l < 32; ++l) q[l] = p[l] + p[l ^ o];
+    for (uint32_t l = 0; l < 32; ++l) p[l] = q[l];
+  }
+  return p[0];
+}
+}  // namespace
+
+int orc_plusplus(const float* X, uint64_t n, uint32_t d, uint32_t k, int seed, int nthreads,
+                 int64_t* picks) {
+  const uint32_t s = 2u + (uint32_t)std::ceil(std::log((double)k));
+  if (s > 16 || n == 0 || k == 0) return 1;
+  std::mt19937_64 gen((uint64_t)(int64_t)seed);
+  std::uniform_real_distribution<double> uni(0.0, 1.0);
+  const uint64_t first = std::uniform_int_distribution<uint64_t>(0, n - 1)(gen);
+  std::vector<double> hu((size_t)(k > 1 ? k - 1 : 1) * s);
+  for (auto& v : hu) v = uni(gen);
+  std::vector<float> d2(n), D((size_t)n * s);
+  parallel_for(nthreads, n, [&](int, uint64_t b, uint64_t e) {
+    for (uint64_t i = b; i < e; ++i) d2[i] = pp_dist32(X + i * d, X + first * d, d);
+  });
+  picks[0] = (int64_t)first;
+  std::vector<uint64_t> cand(s);
+  const int nt = std::max(1, nthreads);
+  for (uint32_t r = 1; r < k; ++r) {
+    double tot = 0.0;
+    for (uint64_t i = 0; i < n; ++i) tot += (double)d2[i];
+    for (uint32_t j = 0; j < s; ++j) {
+      const double u = hu[(size_t)(r - 1) * s + j];
+      if (!(tot > 0.0)) {
+        cand[j] = std::min<uint64_t>(n - 1, (uint64_t)(u * (double)n));
+        continue;
+      }
+      const double target = u * tot;
+      double acc = 0.0;
+      uint64_t pick = UINT64_MAX, last = 0;
+      for (uint64_t i = 0; i < n; ++i) {
+        if (!(d2[i] > 0.0f)) continue;
+        last = i;
+        acc += (double)d2[i];
+        if (acc > target) { pick = i; break; }
+      }
+      cand[j] = pick == UINT64_MAX ? last : pick;
+    }
+    std::vector<double> part((size_t)nt * s, 0.0);
+    parallel_for(nthreads, n, [&](int t, uint64_t b, uint64_t e) {
+      for (uint64_t i = b; i < e; ++i)
+        for (uint32_t j = 0; j < s; ++j) {
+          const float v = pp_dist32(X + i * d, X + cand[j] * d, d);
+          D[i * s + j] = v;
+          part[(size_t)t * s + j] += (double)std::fmin(v, d2[i]);
+        }
+    });
+    uint32_t best = 0;
+    double bestv = 0.0;
+    for (uint32_t j = 0; j < s; ++j) {
+      double c = 0.0;
+      for (int t = 0; t < nt; ++t) c += part[(size_t)t * s + j];
+      if (j == 0 || c < bestv) { bestv = c; best = j; }
+    }
+    picks[r] = (int64_t)cand[best];
+    for (uint64_t i = 0; i < n; ++i) d2[i] = std::fmin(d2[i], D[i * s + best]);
+  }
+  return 0;
+}
+
 // FP64 k-means objective sum_i ||x_i - c_{label_i}||^2 for float centroids.
 double orc_inertia(const float* X, const uint32_t* labels, const float* C, uint64_t n, uint32_t d,
                    uint32_t k, int nthreads) {

@@ -71,6 +71,8 @@ def oracle():
         lib.orc_lloyd_f64_obj.restype = u64
         lib.orc_lloyd_f64_obj.argtypes = [vp, u64, u32, u32, C.c_double, i32, u64, vp, i32, vp, vp,
                                           C.POINTER(u64), C.POINTER(C.c_double)]
+        lib.orc_plusplus.restype = i32
+        lib.orc_plusplus.argtypes = [vp, u64, u32, u32, i32, i32, vp]
         lib.orc_inertia.restype = C.c_double
         lib.orc_inertia.argtypes = [vp, vp, vp, u64, u32, u32, i32]
         lib.orc_kernel_matrix.restype = None
@@ -121,6 +123,16 @@ def orc_lloyd64_obj(X, k, tol, seed, maxiter, C0=None, threads=8):
                                     None if c0 is None else c0.ctypes.data, threads, lab.ctypes.data,
                                     cen.ctypes.data, C.byref(ex), C.byref(obj))
     return int(it), lab, cen, int(ex.value), float(obj.value)
+
+
+def orc_plusplus(X, k, seed, threads=8):
+    """The oracle's seeded greedy k-means++: the k picked row indices."""
+    X = np.ascontiguousarray(X, np.float32)
+    picks = np.empty(k, np.int64)
+    rc = oracle().orc_plusplus(X.ctypes.data, X.shape[0], X.shape[1], k, seed, threads, picks.ctypes.data)
+    if rc != 0:
+        raise ValueError("orc_plusplus: unsupported k")
+    return picks
 
 
 def orc_assign(X, Cc, threads=8):

@@ -1,9 +1,12 @@
 """Greedy k-means++ initialisation (KM_INIT_PLUSPLUS; the reference's
 init_centroids_plus_plus, src/kmeans.cu:447-769).  The reference draws from
-std::random_device, so there is no sequence to match; the tests check the
-properties the algorithm guarantees: seeded determinism, centroids that are
-distinct data points, D^2 sampling that covers well-separated blobs, and a
-lower starting cost than sample picks."""
+std::random_device, so no sequence of its own can be matched; the device's
+seeded draws are restated in the oracle (orc_plusplus: the same RNG stream,
+s = 2 + ceil(ln k) candidates, FP64 prefix sums, the lowest total cost) and
+the picked rows must be identical.  Beside that, the properties the algorithm
+guarantees: seeded determinism, centroids that are distinct data points, D^2
+sampling that covers well-separated blobs, a lower starting cost than sample
+picks."""
 import numpy as np
 import pytest
 
@@ -66,3 +69,14 @@ def test_plusplus_fit_converges(km, gpu):
     m.close()
     assert r.converged and r.iterations < 100
     assert lab.max() < 16
+
+
+@pytest.mark.parametrize("n,d,k,seed", [(20000, 16, 40, 7), (7001, 37, 100, 3), (50000, 128, 256, 11),
+                                        (3000, 3, 2, 0), (1000, 64, 1, 5)])
+def test_plusplus_picks_match_oracle(km, gpu, n, d, k, seed):
+    """The centroids are exactly the rows the oracle's restatement picks."""
+    X, _ = helpers.synth_blobs_np(n, d, max(2, k // 2), -10, 10, 1.0, 100 + seed)
+    C = pp_centroids(km, X, k, seed)
+    picks = helpers.orc_plusplus(X, k, seed)
+    np.testing.assert_array_equal(C.view(np.uint32), X[picks].view(np.uint32))
+

@@ -191,3 +191,20 @@ def test_kkm_step_blocked_matches_oracle_iteration(kind, params):
     assert abs(score - sc.value) <= 1e-9 * max(1.0, abs(sc.value))
     diag = ks.kernel_diag(X, kind, gamma, coef, degree, sigma)
     np.testing.assert_allclose(diag, np.diagonal(K), rtol=1e-12, atol=1e-12)
+
+
+def test_plusplus_oracle_properties():
+    """The oracle's seeded k-means++: deterministic per seed, k distinct rows on
+    separated blobs, one pick per blob (D^2 sampling), and a cost well below
+    uniform sample picks."""
+    X, blob = helpers.synth_blobs_np(8000, 6, 24, -100, 100, 0.5, 3)
+    a = helpers.orc_plusplus(X, 24, 9)
+    b = helpers.orc_plusplus(X, 24, 9)
+    c = helpers.orc_plusplus(X, 24, 10)
+    np.testing.assert_array_equal(a, b)
+    assert not np.array_equal(a, c)
+    assert len(set(a.tolist())) == 24
+    assert len({int(blob[i]) for i in a}) >= 22
+    d2 = lambda C: float(((X[:, None, :].astype(np.float64) - C[None].astype(np.float64)) ** 2).sum(2).min(1).sum())
+    rc, sp = helpers.orc_sample_picks(X, 24, 9)
+    assert d2(X[a]) < 0.5 * d2(X[sp])
