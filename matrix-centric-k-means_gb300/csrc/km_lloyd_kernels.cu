@@ -1086,9 +1086,16 @@ update_sums_kernel(const float* __restrict__ X, const uint32_t* __restrict__ per
 // (a long-latency operation on this GPU).  Every wait is bounded; on timeout
 // the CTA flags KM_DEVERR_TIMEOUT and drains its copies before exiting.
 // Permutation indices are prefetched P batches ahead in registers consumed in
-// place.
+// place.  A batch is BLK_ROWS = 128 rows (four groups of 32): every batch costs
+// the consumer one wait and one release of fixed latency, which at 32 rows per
+// batch capped a CTA at about 140 rows/us (measured); at 128 rows the largest
+// clusters' chains run at about 280 rows/us.  BLK_STAGES is a multiple of
+// BLK_PROD, so a stage is always refilled by the same producer, which waits on
+// its phases in order (a parity wait can never alias a later phase).
 namespace {
-constexpr int BLK_ROWS = 32, BLK_STAGES = 16, BLK_COLS = 32, BLK_PROD = 3;
+constexpr int BLK_ROWS = 128, BLK_GRP = 32, BLK_STAGES = 6, BLK_COLS = 32, BLK_PROD = 3;
+static_assert(BLK_STAGES % BLK_PROD == 0, "a stage must always belong to the same producer");
+static_assert(BLK_ROWS % BLK_GRP == 0, "batches are whole groups of 32 rows");
 constexpr uint64_t BLK_WAIT_NS = 2000000000ull;
 constexpr uint32_t BLK_SUSPEND_NS = 2000;       // try_wait suspend hint
 constexpr size_t BLK_SMEM = (size_t)BLK_STAGES * BLK_ROWS * BLK_COLS * sizeof(float);
@@ -1130,14 +1137,18 @@ update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict_
   };
 
   if (warp < BLK_PROD) {
-    constexpr int P = 4;
+    constexpr int P = 2;                       // batches of indices prefetched per producer
+    constexpr int G = BLK_ROWS / BLK_GRP;
     const uint32_t p0 = (uint32_t)warp;
-    uint32_t pq[P];
+    uint32_t pq[P][G];
 #pragma unroll
     for (int i = 0; i < P; ++i) {
       const uint32_t b = p0 + (uint32_t)i * BLK_PROD;
-      const uint32_t idx = s0 + b * BLK_ROWS + (uint32_t)lane;
-      pq[i] = (b < nb && idx < s1) ? perm[idx] : 0u;
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const uint32_t idx = s0 + b * BLK_ROWS + (uint32_t)(g * BLK_GRP) + (uint32_t)lane;
+        pq[i][g] = (b < nb && idx < s1) ? perm[idx] : 0u;
+      }
     }
     // Unrolled by P so that pq[i] is consumed in place, P batches after its
     // load was issued (moving a register whose load is in flight would wait).
@@ -1151,30 +1162,36 @@ update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict_
         const bool okw = mbar_wait_bounded(&empty[s], ph ^ 1u, ab, BLK_WAIT_NS, BLK_SUSPEND_NS);
         if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(); ok = false; break; }
         const uint32_t m = min((uint32_t)BLK_ROWS, s1 - (s0 + b * BLK_ROWS));
-        const uint32_t rl = pq[i];
         // One instruction copies BLK_RPI rows: BLK_LPR lanes of 16 bytes per
         // row; columns past w and rows past m zero-fill.
         const uint32_t sub = (uint32_t)lane / BLK_LPR, c4 = ((uint32_t)lane % BLK_LPR) * 4u;
         const bool lane_has_cols = c4 < w;
-        float* dst = ring + ((size_t)s * BLK_ROWS + sub) * BLK_COLS + c4;
-        // All row indices first: each cp.async is an ordered asm statement, so
-        // a shuffle placed between two of them would put its latency on every row.
-        uint32_t rr[BLK_ROWS / BLK_RPI];
-#pragma unroll
-        for (int ii = 0; ii < BLK_ROWS / BLK_RPI; ++ii)
-          rr[ii] = __shfl_sync(0xffffffffu, rl, ii * BLK_RPI + (int)sub);
         const float* xl = X + j0 + c4;
 #pragma unroll
-        for (int ii = 0; ii < BLK_ROWS / BLK_RPI; ++ii) {
-          const uint32_t u = (uint32_t)ii * BLK_RPI + sub;
-          const bool okr = u < m && lane_has_cols;
-          const float* src = okr ? xl + (uint64_t)rr[ii] * d : X;
-          cp_async16_zfill(dst + (size_t)ii * BLK_RPI * BLK_COLS, src, okr ? 16u : 0u);
+        for (int g = 0; g < G; ++g) {
+          float* dst = ring + ((size_t)s * BLK_ROWS + (size_t)(g * BLK_GRP) + sub) * BLK_COLS + c4;
+          // All row indices of the group first: each cp.async is an ordered asm
+          // statement, so a shuffle placed between two of them would put its
+          // latency on every row.
+          uint32_t rr[BLK_GRP / BLK_RPI];
+#pragma unroll
+          for (int ii = 0; ii < BLK_GRP / BLK_RPI; ++ii)
+            rr[ii] = __shfl_sync(0xffffffffu, pq[i][g], ii * BLK_RPI + (int)sub);
+#pragma unroll
+          for (int ii = 0; ii < BLK_GRP / BLK_RPI; ++ii) {
+            const uint32_t u = (uint32_t)(g * BLK_GRP + ii * BLK_RPI) + sub;
+            const bool okr = u < m && lane_has_cols;
+            const float* src = okr ? xl + (uint64_t)rr[ii] * d : X;
+            cp_async16_zfill(dst + (size_t)ii * BLK_RPI * BLK_COLS, src, okr ? 16u : 0u);
+          }
         }
         cp_async_mbar_arrive_noinc(&full[s]);
         const uint32_t nbb = b + (uint32_t)P * BLK_PROD;
-        const uint32_t idx = s0 + nbb * BLK_ROWS + (uint32_t)lane;
-        pq[i] = (nbb < nb && idx < s1) ? perm[idx] : 0u;
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+          const uint32_t idx = s0 + nbb * BLK_ROWS + (uint32_t)(g * BLK_GRP) + (uint32_t)lane;
+          pq[i][g] = (nbb < nb && idx < s1) ? perm[idx] : 0u;
+        }
       }
     }
     // Drain: this warp's copies must land before the CTA exits.
@@ -1191,33 +1208,38 @@ update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict_
       const bool ok = mbar_wait_bounded(&full[s], ph, ab, BLK_WAIT_NS, BLK_SUSPEND_NS);
       if (!__all_sync(0xffffffffu, ok)) { if (lane == 0) fail(); break; }
       const uint32_t m = min((uint32_t)BLK_ROWS, s1 - (s0 + b * BLK_ROWS));
-      const float* src = ring + (size_t)s * BLK_ROWS * BLK_COLS + col;
-      float e32 = 0.0f, e32b = 0.0f;
-      if (m == (uint32_t)BLK_ROWS) {
-        // Full batch: all loads first, then the ordered chain (no branch or
-        // load latency on the dependent additions).
-        float v[BLK_ROWS];
+      // Groups of 32 rows in order; the group's objective partial joins the
+      // FP32 pair, as one batch of 32 rows did.
+      for (uint32_t g0 = 0; g0 < m; g0 += BLK_GRP) {
+        const uint32_t mg = min((uint32_t)BLK_GRP, m - g0);
+        const float* src = ring + ((size_t)s * BLK_ROWS + g0) * BLK_COLS + col;
+        float e32 = 0.0f, e32b = 0.0f;
+        if (mg == (uint32_t)BLK_GRP) {
+          // Full group: all loads first, then the ordered chain (no branch or
+          // load latency on the dependent additions).
+          float v[BLK_GRP];
 #pragma unroll
-        for (int u = 0; u < BLK_ROWS; ++u) v[u] = vj ? src[(size_t)u * BLK_COLS] : 0.0f;
+          for (int u = 0; u < BLK_GRP; ++u) v[u] = vj ? src[(size_t)u * BLK_COLS] : 0.0f;
 #pragma unroll
-        for (int u = 0; u < BLK_ROWS; ++u) {
-          sum = __fadd_rn(sum, v[u]);
-          const float t = v[u] - cold;
-          if (u & 1) e32b = fmaf(t, t, e32b); else e32 = fmaf(t, t, e32);
+          for (int u = 0; u < BLK_GRP; ++u) {
+            sum = __fadd_rn(sum, v[u]);
+            const float t = v[u] - cold;
+            if (u & 1) e32b = fmaf(t, t, e32b); else e32 = fmaf(t, t, e32);
+          }
+        } else {
+          for (uint32_t u = 0; u < mg; ++u) {
+            const float v = vj ? src[(size_t)u * BLK_COLS] : 0.0f;
+            sum = __fadd_rn(sum, v);
+            const float t = v - cold;
+            e32 = fmaf(t, t, e32);
+          }
         }
-      } else {
-        for (uint32_t u = 0; u < m; ++u) {
-          const float v = vj ? src[(size_t)u * BLK_COLS] : 0.0f;
-          sum = __fadd_rn(sum, v);
-          const float t = v - cold;
-          e32 = fmaf(t, t, e32);
-        }
+        e32 = __fadd_rn(e32, e32b);
+        // TwoSum: eh + e32 = s_ + err exactly; err accumulates into el
+        const float s_ = __fadd_rn(eh, e32), bb = __fsub_rn(s_, eh);
+        el = __fadd_rn(el, __fadd_rn(__fsub_rn(eh, __fsub_rn(s_, bb)), __fsub_rn(e32, bb)));
+        eh = s_;
       }
-      e32 = __fadd_rn(e32, e32b);
-      // TwoSum: eh + e32 = s_ + err exactly; err accumulates into el
-      const float s_ = __fadd_rn(eh, e32), bb = __fsub_rn(s_, eh);
-      el = __fadd_rn(el, __fadd_rn(__fsub_rn(eh, __fsub_rn(s_, bb)), __fsub_rn(e32, bb)));
-      eh = s_;
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);
     }
