@@ -473,14 +473,36 @@ def bigk_arm(args):
         # label agreement after the same iterations from the same seeded start
         m = km.Lloyd(n, d, k, tol=c["tol"], seed=1, maxiter=steps32, precision=args.precision, conv="none",
                      stream=stream.cuda_stream).set_data_bf16(bits)
-        lab_b, _, _ = m.fit(want_centroids=False)
+        lab_b, cen_b, _ = m.fit()
         m.close()
+        lab_all, _, _ = km.assign(Xd, torch.from_numpy(cen_b).cuda(), precision=args.precision)
+        lab_all = lab_all.cpu().numpy().astype(np.uint32)
         m = km.Lloyd(n, d, k, tol=c["tol"], seed=1, maxiter=steps32, precision="fp32", conv="none",
                      stream=stream.cuda_stream).set_data(Xd)
         lab_f, _, _ = m.fit(want_centroids=False)
         m.close()
     agree = float((lab_b == lab_f).mean())
     sizes = np.bincount(lab_b, minlength=k)
+    # Oracle parity: (1) the fit's centroids against the oracle's update of its
+    # labels over all n rows; (2) the assignment of all n rows to those
+    # centroids against the oracle's (reference CPU formula) and against FP64
+    # on 65,536 rows spread over the whole range.
+    Xh = Xd.cpu().numpy()
+    cen_o, _ = helpers.orc_update(Xh, lab_b, k, threads=os.cpu_count() or 8)
+    rows = np.sort(np.random.default_rng(11).choice(n, min(n, 65536), replace=False))
+    lab_s, _ = helpers.orc_assign(Xh[rows], cen_b, threads=os.cpu_count() or 8)
+    X64, C64 = Xh[rows].astype(np.float64), cen_b.astype(np.float64)
+    D64 = (X64 * X64).sum(1)[:, None] - 2.0 * X64 @ C64.T + (C64 * C64).sum(1)[None, :]
+    lab64 = D64.argmin(1)
+    obj_ours = float(D64[np.arange(len(rows)), lab_all[rows]].sum())
+    obj64 = float(D64[np.arange(len(rows)), lab64].sum())
+    parity = {"centroids_bitwise_equal_vs_oracle_update": bool(np.array_equal(cen_b.view(np.uint32),
+                                                                             cen_o.view(np.uint32))),
+              "sample_rows": int(len(rows)),
+              "label_agreement_vs_oracle": float((lab_all[rows] == lab_s).mean()),
+              "label_agreement_vs_fp64": float((lab_all[rows] == lab64).mean()),
+              "objective_rel_err_vs_fp64": abs(obj_ours - obj64) / abs(obj64)}
+    del Xh, X64, D64
     rb = res[args.precision]
     value = rb["iters"] / (rb["ms"] / 1e3)
     v32 = res["fp32"]["iters"] / (res["fp32"]["ms"] / 1e3)
@@ -527,6 +549,9 @@ def bigk_arm(args):
         "fp32_plain": {"value": v32, "unit": "iters/s", "iters": res["fp32"]["iters"]},
         "speedup_vs_fp32_plain": value / v32,
         "label_agreement_vs_fp32": agree,
+        "label_agreement_vs_oracle": parity["label_agreement_vs_oracle"],
+        "objective_rel_err_vs_fp64": parity["objective_rel_err_vs_fp64"],
+        "oracle_parity": parity,
         "refined_rows_per_iter": rb["refined"] / max(1, rb["iters"]),
         "full_rescore_rows_per_iter": rb["full"] / max(1, rb["iters"]),
         "cluster_sizes": {"max": int(sizes.max()), "median": float(np.median(sizes)), "empty": int((sizes == 0).sum())},
@@ -554,7 +579,11 @@ def kkm_arm(args):
     storage, BF16 for BF16 storage)."""
     import torch
     import helpers
+    import importlib.util
     km = helpers.km()
+    spec = importlib.util.spec_from_file_location("kkm_step", ROOT / "oracle" / "kkm_step.py")
+    ks = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(ks)
     c = KKM
     n, d, k = c["n"], c["d"], c["k"]
     X = km.synth_blobs(n, d, k, c["lo"], c["hi"], c["sigma"], c["seed"], nthreads=os.cpu_count() or 8)
@@ -574,7 +603,12 @@ def kkm_arm(args):
             clk = Clocks(0)
             with clk:
                 lab, r = m.fit()
+            # one more iteration from the fit's labels, against the FP64 oracle's
+            km.check(km.lib().km_kkm_configure(m.h, 1, m.p.tol, 0), "km_kkm_configure")
+            lab1, r1 = m.fit(init_labels=lab)
             m.close()
+            new, score = ks.kkm_step_f64(X, lab, k, kern, **params, workers=max(1, (os.cpu_count() or 8) // 2))
+            trace = float(ks.kernel_diag(X, kern, **params).sum())
             torch.cuda.empty_cache()
             ips = r.iterations / (r.fit_ms / 1e3)
             kbytes = n * n * (2 if kb16 else 4)
@@ -583,7 +617,9 @@ def kkm_arm(args):
                 "iters_per_s": ips, "ms_per_iter": it_ms, "k_build_ms": min(kb_ms),
                 "k_build_tflops": 2.0 * n * n * d / (min(kb_ms) / 1e3) / 1e12,
                 "iter_gbs": (kbytes + 4 * n + 4 * n * k) / (it_ms / 1e3) / 1e9,
-                "score": r.score, "clocks": clk.summary(), "launches": r.kernel_launches}
+                "score": r.score, "clocks": clk.summary(), "launches": r.kernel_launches,
+                "one_step_vs_fp64": {"label_agreement": float((lab1 == new).mean()),
+                                     "objective_rel_err": abs((r1.score + trace) - (score + trace)) / abs(score + trace)}}
     head = rows["polynomial/fp32K"]
     # e2e through the public API from host memory: set_data (H2D of X and the
     # K build) + fit + labels D2H, the headline variant
@@ -611,6 +647,10 @@ def kkm_arm(args):
         "config": {"workload": "kernel k-means n=65536 d=512 k=64, polynomial (x.y/d+1)^2, K FP32 16 GiB",
                    "n": n, "d": d, "k": k, "l2": "K larger than L2", "parallelism": "single GPU"},
         "variants": rows,
+        "label_agreement_vs_fp64": head["one_step_vs_fp64"]["label_agreement"],
+        "objective_rel_err_vs_fp64": head["one_step_vs_fp64"]["objective_rel_err"],
+        "oracle_parity_note": "one iteration from the timed fit's labels against the FP64 oracle (K formed block "
+                              "by block), per variant; the reference GPU path itself cannot be built here",
         "roofline": {"bound": "hbm", "achieved": head["iter_gbs"], "peak": hbm, "unit": "GB/s",
                      "frac": head["iter_gbs"] / hbm, "kernel": "kkm_vk_kernel (V.K streaming of K)",
                      "peak_source": src, "traffic": None},
@@ -709,15 +749,9 @@ def batch_arm(args):
     single-problem fits (the FP32 Lloyd handle, one instance after another)."""
     import helpers
     km = helpers.km()
-    rng = np.random.default_rng(4000)
     P, R = 512, 8
-    shapes, Xs = [], []
-    for p in range(P):
-        n = int(np.exp(rng.uniform(np.log(1024), np.log(65536))))
-        d = int(rng.choice([2, 8, 16, 32, 64, 128, 256]))
-        k = min(int(rng.integers(2, 129)), n - 1)
-        shapes.append((n, d, k))
-        Xs.append(km.synth_blobs(n, d, k, -5.0, 5.0, 1.0, 4000 + p, nthreads=os.cpu_count() or 8))
+    shapes = helpers.batch_problems(P)
+    Xs = helpers.batch_points(shapes, nthreads=os.cpu_count() or 8)
     b = km.Batch(shapes, restarts=R, seed=0, tol=1e-4, maxiter=300).set_data(Xs)
     v, tune_ms = b.tune()
     b.fit()                                          # warm-up
@@ -739,6 +773,30 @@ def batch_arm(args):
            "step": f"set_data of all {P} problems from host memory + one batched fit with results to the host; "
                    f"wall clock {e2e_s * 1e3:.1f} ms"}
     iters = sum(r[1] for pr in results for r in pr)
+    # Oracle parity on the full-size problems: the four largest (n*d*k) and
+    # twelve seeded others, restart 0 and the last restart of each.
+    work = np.array([n * d * k for n, d, k in shapes])
+    big = [int(p) for p in np.argsort(work)[::-1][:4]]
+    others = [int(p) for p in np.random.default_rng(5).permutation(P) if int(p) not in big][:12]
+    b2 = km.Batch(shapes, restarts=R, seed=0, tol=1e-4, maxiter=300).set_data(Xs)
+    b2.fit()
+    same, checked = 0, 0
+    for p in big + others:
+        n, d, k = shapes[p]
+        for r in (0, R - 1):
+            it_o, lab_o, cen_o, _ = helpers.orc_lloyd(Xs[p], k, 1e-4, p * R + r, 300, threads=os.cpu_count() or 8)
+            lab, cen = b2.instance(p, r)
+            same += int(np.array_equal(lab, lab_o) and np.array_equal(cen.view(np.uint32), cen_o.view(np.uint32))
+                        and results[p][r][0] == it_o)
+            checked += 1
+    b2.close()
+    # the assignment's arithmetic: 3 FP32 operations (sub, mul, add: the
+    # reference formula, no FMA) per point, centroid and coordinate, per
+    # iteration of every instance
+    ops = 3.0 * sum(results[p][r][1] * shapes[p][0] * shapes[p][1] * shapes[p][2]
+                    for p in range(P) for r in range(R))
+    fp32_peak = 152 * 128 * 2.07e9 / 1e12          # nominal FP32 instructions/s (T/s)
+    ach = ops / (ms / 1e3) / 1e12
     # sequential per-problem loop on a sample of problems (all restarts), scaled
     sample = list(range(0, P, P // 16))[:16]
     t0 = time.perf_counter()
@@ -769,6 +827,14 @@ def batch_arm(args):
                             "sample_work_fraction": seq_frac,
                             "note": "km_lloyd FP32 handle per instance, one after another, same seeds"},
         "speedup_vs_sequential": value / seq_pps,
+        "oracle_parity": {"instances_checked": checked, "instances_identical": same,
+                          "label_agreement_vs_oracle": same / checked,
+                          "what": "labels, centroids bit for bit and the returned iteration against the oracle's "
+                                  "single run, the 4 largest and 12 other problems, restarts 0 and 7"},
+        "roofline": {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "T FP32 instr/s",
+                     "frac": ach / fp32_peak, "kernel": "batch_lloyd_kernel (exact reference-formula assignment)",
+                     "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2.07 GHz; no measured FP32 figure)",
+                     "traffic": None},
         "clocks": clk.summary(), "gpu_launches": 1, "e2e": e2e,
     }
 

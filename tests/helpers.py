@@ -339,6 +339,26 @@ def synth_blobs_np_chunked(n, d, blobs, lo, hi, sigma, seed, rows_per_chunk=6553
     return out, lab
 
 
+def batch_problems(count=512, seed=4000):
+    """Shapes of the batched workload: n log-uniform in [1024, 65536], d in
+    {2, 8, 16, 32, 64, 128, 256}, k uniform in [2, 128] (k < n)."""
+    rng = np.random.default_rng(seed)
+    shapes = []
+    for _ in range(count):
+        n = int(np.exp(rng.uniform(np.log(1024), np.log(65536))))
+        d = int(rng.choice([2, 8, 16, 32, 64, 128, 256]))
+        k = min(int(rng.integers(2, 129)), n - 1)
+        shapes.append((n, d, k))
+    return shapes
+
+
+def batch_points(shapes, seed=4000, nthreads=8):
+    """Points of the batched workload: problem p is one seeded Gaussian blob
+    per cluster (sigma 1, centers U[-5,5]^d), seed + p."""
+    return [km().synth_blobs(n, d, k, -5.0, 5.0, 1.0, seed + p, nthreads=nthreads)
+            for p, (n, d, k) in enumerate(shapes)]
+
+
 def config1_data(seed=0):
     """Plain Lloyd workload: n=1797, d=64, k=10 blobs, centers U[0,16]^64,
     sigma=3, rounded and clipped to [0,16] (integer-valued floats)."""

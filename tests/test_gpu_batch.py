@@ -63,3 +63,30 @@ def test_batch_rejects_bad_shapes(km, gpu):
     with pytest.raises(km.KmError) as e:
         km.Batch([(5000, 512, 128)])          # centroids beyond the shared-memory limit
     assert e.value.status == km.KM_ERR_UNSUPPORTED
+
+
+def test_batch_full_workload_matches_oracle(km, gpu):
+    """The full batched workload (512 problems, n up to 65,536, d up to 256,
+    k up to 128, 8 restarts each, all 4096 instances in one launch): the eight
+    largest problems (n*d*k) in all restarts and 24 others in two restarts
+    each equal the oracle's single runs bit for bit (labels, centroids,
+    returned iteration)."""
+    shapes = helpers.batch_problems(512)
+    Xs = helpers.batch_points(shapes)
+    R, tol, maxiter = 8, 1e-4, 300
+    b = km.Batch(shapes, restarts=R, seed=0, tol=tol, maxiter=maxiter).set_data(Xs)
+    best, results, ms = b.fit()
+    work = np.array([n * d * k for n, d, k in shapes])
+    big = [int(p) for p in np.argsort(work)[::-1][:8]]
+    rng = np.random.default_rng(5)
+    rest = [int(p) for p in rng.permutation(512) if int(p) not in big][:24]
+    checks = [(p, r) for p in big for r in range(R)] + [(p, r) for p in rest for r in (0, R - 1)]
+    for p, r in checks:
+        n, d, k = shapes[p]
+        it_o, lab_o, cen_o, ex_o = helpers.orc_lloyd(Xs[p], k, tol, p * R + r, maxiter, threads=16)
+        lab, cen = b.instance(p, r)
+        np.testing.assert_array_equal(lab, lab_o, err_msg=f"problem {p} restart {r} {shapes[p]}")
+        np.testing.assert_array_equal(cen.view(np.uint32), cen_o.view(np.uint32))
+        conv, iters, _ = results[p][r]
+        assert conv == it_o and iters == ex_o
+    b.close()
