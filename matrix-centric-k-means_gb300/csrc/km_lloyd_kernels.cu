@@ -132,8 +132,12 @@ namespace {
 constexpr int SM_ = 128, SN_ = 128, SK_ = 16, SPAD = 4;
 }
 
+// Thread (tx, ty) of the 16 x 16 grid owns rows ty*8 .. ty*8+7 and the two
+// column quads tx*4 .. tx*4+3 and 64 + tx*4 .. +3 of the 128 x 128 tile: the
+// quarter-warps' 16-byte centroid loads from shared memory then cover 128
+// contiguous bytes (no bank conflicts), and two CTAs fit an SM.
 template <bool V4>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(256, 2)
 assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
                   const float* __restrict__ cn2, const float* __restrict__ xn2, uint64_t n,
                   uint32_t d, uint32_t k, TieBound tb, DevState* st,
@@ -237,8 +241,8 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
       for (int kk = 0; kk < SK_; ++kk) {
         const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 8]);
         const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 8 + 4]);
-        const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 8]);
-        const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 8 + 4]);
+        const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
+        const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][kk][64 + tx * 4]);
         const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
         const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
@@ -259,8 +263,9 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
       t.init();
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const uint32_t col = c0 + tx * 8 + j;
-        const float v = fmaf(-2.0f, acc[i][j], cns[tx * 8 + j]);
+        const uint32_t cl = (j < 4) ? (uint32_t)(tx * 4 + j) : (uint32_t)(64 + tx * 4 + j - 4);
+        const uint32_t col = c0 + cl;
+        const float v = fmaf(-2.0f, acc[i][j], cns[cl]);
         if (Dout && row < n && col < k) Dout[row * k + col] = v + xn2[row];
         if (col < k) t.insert_nb(v, col);
       }
