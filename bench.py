@@ -10,8 +10,9 @@ convergence and objective reductions.
                     [--precision bf16|bf16x3|fp32]
 
 --impl ours (default) prints one JSON line: `value` = iterations/s of the
-BF16 tensor-core + exact-refinement path (FP32 accumulate; --precision bf16x3
-for the split form hi*hi + hi*lo + lo*hi) with the points resident in HBM
+split-BF16x3 tensor-core + exact-refinement path (hi*hi + hi*lo + lo*hi,
+FP32 accumulate; --precision bf16 for the single-BF16 form) with the points
+resident in HBM
 (device-timed with CUDA events on the launching stream), the FP32 plain path
 beside it, labels compared between the two, `roofline` for the dominant kernel,
 `e2e` through the C ABI from pinned host memory, `cpu_baseline` (the oracle port
@@ -864,9 +865,10 @@ def main():
                          "~0.4 ms, so that clock samples fall inside the timed region; 20 otherwise)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default=None, choices=["bf16", "bf16x3", "fp32"],
-                    help="tensor-core form of the timed arm (default: bf16 for lloyd, the faster form "
-                         "there; bf16x3 for bigk, whose BF16-stored points take the two-term split)")
+    ap.add_argument("--precision", default="bf16x3", choices=["bf16", "bf16x3", "fp32"],
+                    help="tensor-core form of the timed arm (default bf16x3: the faster form end to end, "
+                         "a fit from its seeded start; single BF16 is faster once the centroids settle; "
+                         "for bigk's BF16-stored points bf16x3 is the two-term split)")
     ap.add_argument("--workload", default="lloyd", choices=["lloyd", "bigk", "kkm", "kkm-panel", "batch"],
                     help="lloyd: the headline n=1M d=128 k=256 workload (default); bigk: n=4M d=256 "
                          "k=4096 BF16 points; kkm: kernel k-means n=65536 d=512 k=64; kkm-panel: kernel "
@@ -883,8 +885,6 @@ def main():
         args.steps = (200 if (args.workload == "lloyd" and args.impl == "ours")
                       else 5 if args.workload == "kkm-panel" else 20)
     args.warmup = max(args.warmup, 3)
-    if args.precision is None:
-        args.precision = "bf16x3" if args.workload == "bigk" else "bf16"
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

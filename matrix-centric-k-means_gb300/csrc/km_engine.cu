@@ -80,6 +80,9 @@ LloydEngine::~LloydEngine() {
   dfree(q2); dfree(q2full); dfree(q2cnt); dfree(q2fcnt); dfree(fidx); dfree(nfull);
   dfree(seghist); dfree(counts); dfree(cstart); dfree(order); dfree(perm); dfree(red_part); dfree(st);
   if (h_st) cudaFreeHost(h_st);
+  if (aux) cudaStreamDestroy(aux);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -205,10 +208,14 @@ km_status LloydEngine::init(uint64_t n_, uint32_t d_, uint32_t k_, int precision
 
 km_status LloydEngine::set_points(const float* Xsrc, bool on_device, bool copy) {
   KM_CUDA_TRY(cudaSetDevice(device));
+  const size_t bytes = sizeof(float) * n * d;
+  // A large host source is copied in row chunks alternating between the
+  // handle's stream and a second one (two copy engines), and each chunk's
+  // preparation (norms, BF16 copies) runs behind its own copy, overlapping
+  // the copies of the chunks after it.
+  const bool chunked = !on_device && bytes >= (64ull << 20);
   if (copy || !on_device) {
     if (!X_owned) KM_TRY(dalloc(&X_owned, (size_t)n * d));
-    KM_CUDA_TRY(cudaMemcpyAsync(X_owned, Xsrc, sizeof(float) * n * d,
-                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
     X = X_owned;
   } else {
     X = Xsrc;
@@ -216,8 +223,34 @@ km_status LloydEngine::set_points(const float* Xsrc, bool on_device, bool copy) 
   refine_v4 = (d % 4 == 0) && (reinterpret_cast<uintptr_t>(X) % 16 == 0);
   KM_CUDA_TRY(cudaMemsetAsync(&st->err, 0, sizeof(uint32_t), stream));
   KM_CUDA_TRY(cudaMemsetAsync(&st->x_not_bf16, 0, sizeof(uint32_t), stream));
-  const int blocks = (int)std::min<uint64_t>((n + 7) / 8, (uint64_t)num_sms * 16);
-  prep_points_kernel<<<blocks, 256, 0, stream>>>(X, n, d, dp, xn2, xn2d, Xb, Xlo, st);
+  if (chunked) {
+    if (!aux) {
+      KM_CUDA_TRY(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+      KM_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+      KM_CUDA_TRY(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    }
+    KM_CUDA_TRY(cudaEventRecord(ev_fork, stream));
+    KM_CUDA_TRY(cudaStreamWaitEvent(aux, ev_fork, 0));
+    const uint64_t nch = 8, rows = (n + nch - 1) / nch;
+    for (uint64_t c = 0; c < nch; ++c) {
+      const uint64_t r0 = c * rows, r1 = std::min<uint64_t>(n, r0 + rows);
+      if (r0 >= r1) break;
+      cudaStream_t sc = (c & 1) ? aux : stream;
+      KM_CUDA_TRY(cudaMemcpyAsync(X_owned + r0 * d, Xsrc + r0 * d, sizeof(float) * (r1 - r0) * d,
+                                  cudaMemcpyHostToDevice, sc));
+      const int blocks = (int)std::min<uint64_t>((r1 - r0 + 7) / 8, (uint64_t)num_sms * 8);
+      prep_points_kernel<<<blocks, 256, 0, sc>>>(X + r0 * d, r1 - r0, d, dp, xn2 + r0, xn2d + r0,
+                                                 Xb ? Xb + r0 * dp : nullptr, Xlo ? Xlo + r0 * dp : nullptr, st);
+    }
+    KM_CUDA_TRY(cudaEventRecord(ev_join, aux));
+    KM_CUDA_TRY(cudaStreamWaitEvent(stream, ev_join, 0));
+  } else {
+    if (copy || !on_device)
+      KM_CUDA_TRY(cudaMemcpyAsync(X_owned, Xsrc, bytes,
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
+    const int blocks = (int)std::min<uint64_t>((n + 7) / 8, (uint64_t)num_sms * 16);
+    prep_points_kernel<<<blocks, 256, 0, stream>>>(X, n, d, dp, xn2, xn2d, Xb, Xlo, st);
+  }
   KM_CUDA_TRY(cudaGetLastError());
   reduce_f64_partial_kernel<<<256, 256, 0, stream>>>(xn2d, n, red_part);
   reduce_f64_final_kernel<<<1, 32, 0, stream>>>(red_part, 256, &st->sum_x2);

@@ -87,6 +87,8 @@ struct LloydEngine {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaStream_t aux = nullptr;           // second stream of the chunked host-to-device copy
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int num_sms = 0;
   uint64_t n = 0;
   uint32_t d = 0, k = 0, dp = 0, kp = 0;

@@ -35,22 +35,37 @@ __global__ void prep_points_kernel(const float* __restrict__ X, uint64_t n, uint
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  // ||x||^2 as an unevaluated FP32 pair (hi + lo): each square split exactly
+  // by an FMA, each addition by TwoSum (the FP64 units of this GPU are a
+  // small fraction of its FP32 rate); the pair is within a few units of 2^-48
+  // of the exact value, and float(hi + lo) is the correctly rounded norm.
+  auto two_sum = [](float& h, float& l, float a, float al) {
+    const float t = __fadd_rn(h, a), bp = __fsub_rn(t, h);
+    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(t, bp)), __fsub_rn(a, bp));
+    h = t;
+    l = __fadd_rn(l, __fadd_rn(al, err));
+  };
   for (uint64_t r = warp; r < n; r += nw) {
     const float* x = X + r * d;
-    double s = 0.0;
+    float sh = 0.0f, sl = 0.0f;
     bool bad = false, inexact = false;
     for (uint32_t j = lane; j < dp; j += 32) {
       float v = (j < d) ? x[j] : 0.0f;
       if (!isfinite(v)) bad = true;
       if ((__float_as_uint(v) & 0xffffu) != 0u) inexact = true;    // not a BF16 value
-      s += (double)v * (double)v;
+      const float p = __fmul_rn(v, v);
+      two_sum(sh, sl, p, fmaf(v, v, -p));
       if (Xb) {
         __nv_bfloat16 hi = __float2bfloat16_rn(v);
         Xb[r * dp + j] = hi;
         if (Xlo) Xlo[r * dp + j] = __float2bfloat16_rn(v - __bfloat162float(hi));
       }
     }
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, sh, o), ol = __shfl_xor_sync(0xffffffffu, sl, o);
+      two_sum(sh, sl, oh, ol);
+    }
+    const double s = (double)sh + (double)sl;
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&st->err, KM_DEVERR_NONFINITE);
     if (__any_sync(0xffffffffu, inexact) && lane == 0) atomicOr(&st->x_not_bf16, 1u);
     if (lane == 0) {
