@@ -80,6 +80,8 @@ LloydEngine::~LloydEngine() {
   dfree(q2); dfree(q2full); dfree(q2cnt); dfree(q2fcnt); dfree(fidx); dfree(nfull);
   dfree(seghist); dfree(counts); dfree(cstart); dfree(order); dfree(perm); dfree(red_part); dfree(st);
   if (h_st) cudaFreeHost(h_st);
+  for (auto& l : kmat_lists)
+    if (l.dev) cudaFree(l.dev);
   if (aux) cudaStreamDestroy(aux);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);

@@ -58,6 +58,7 @@ __device__ __forceinline__ float kfn_apply_k(const KFn& f, float dot, float ni, 
     return dot;
   } else if constexpr (KIND == KM_KERNEL_POLY) {
     const float b = fmaf(f.gamma, dot, f.coef);
+    if (f.degree == 2) return b * b;          // the loop's 1 * b * b, without the loop
     float r = 1.0f;
 #pragma unroll 1
     for (int e = 0; e < f.degree; ++e) r *= b;
@@ -166,6 +167,18 @@ kmat_f32_kernel(const float* __restrict__ X, const float* __restrict__ xn2, uint
 // draining this CTA's copies and MMAs.  The kernel builds rows
 // [prow0, prow_end) of K into K (row stride n, first row = prow0): all of K,
 // or one panel of it; with skip_done it does nothing once the fit has stopped.
+//
+// Symmetry: K is symmetric, so only tiles (row tile mi, column block nj) with
+// mi/2 <= nj are computed (the 256-row blocks on or above the diagonal), as
+// the reference's SYRK path builds one triangle and mirrors it
+// (src/kernels/kernels.cuh:596-649).  A tile strictly above the diagonal
+// (mi/2 < nj) also stores its transpose: each warp holds 32 consecutive rows
+// in its lanes, so column c of the tile leaves as one contiguous run of row
+// c of K.  The tiles come from a list built on the host (kmat_tile_list):
+// (mi, nj | direct << 30 | mirror << 31), `direct` when the tile's own rows
+// lie in [prow0, prow_end) and `mirror` when its transposed rows do, so a
+// panel receives exactly the values the whole matrix holds.  This halves the
+// MMA work of a resident build.
 // ---------------------------------------------------------------------------
 namespace {
 constexpr int KM_M = 128, KM_N = 256;
@@ -175,12 +188,6 @@ constexpr uint64_t KWAIT_NS = 2000000000ull;
 
 constexpr uint64_t KM_GROUP = 16;   // row tiles per raster group of the kernel-matrix build
 
-__device__ __forceinline__ void kmat_tile(uint64_t tile, uint64_t mt, uint64_t nt, uint64_t& mi, uint64_t& nj) {
-  const uint64_t g = tile / (KM_GROUP * nt), r = tile % (KM_GROUP * nt);
-  const uint64_t rows = (mt - g * KM_GROUP) < KM_GROUP ? (mt - g * KM_GROUP) : KM_GROUP;   // last group
-  nj = r / rows;
-  mi = g * KM_GROUP + r % rows;
-}
 
 constexpr uint32_t KM_STG_BYTES = 8u * 32u * 32u * 4u;   // epilogue staging tiles, one per epilogue warp
 
@@ -201,7 +208,7 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
                const __grid_constant__ CUtensorMap tB, const __grid_constant__ CUtensorMap tBlo,
                const float* __restrict__ xn2, uint64_t n, uint64_t prow0, uint64_t prow_end, uint32_t KB,
                uint32_t S, KFn f, void* __restrict__ K, float* __restrict__ diag, int vec, int skip_done,
-               DevState* st) {
+               DevState* st, const uint32_t* __restrict__ tlist, uint64_t ntiles) {
   if (skip_done && st->done) return;   // uniform over the grid: written by an earlier launch
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -210,8 +217,6 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
   float* stg_all = reinterpret_cast<float*>(smem + (size_t)S * stage_bytes);    // [8 warps][32][32]
   KmSmem* ts = reinterpret_cast<KmSmem*>(smem + (size_t)S * stage_bytes + KM_STG_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint64_t mt = (prow_end - prow0 + KM_M - 1) / KM_M, nt = (n + KM_N - 1) / KM_N;
-  const uint64_t ntiles = mt * nt;
   if (threadIdx.x == 0) {
     for (uint32_t s = 0; s < S; ++s) { mbar_init(&ts->full[s], 1); mbar_init(&ts->empty[s], 1); }
     for (int b = 0; b < 2; ++b) { mbar_init(&ts->tfull[b], 1); mbar_init(&ts->tempty[b], 4); }
@@ -229,24 +234,23 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
     ts->abort = 1;
     if (atomicOr(&st->err, KM_DEVERR_TIMEOUT) == 0u) st->err_where = 100u + where;
   };
-  // tile t -> (mi, nj): groups of KM_GROUP row tiles, column tiles in the
-  // inner loop, so that a group's A tiles stay in L2 while X streams once per group
+  // tile t -> (mi, nj) from the list (groups of KM_GROUP row tiles, column
+  // blocks in the inner loop, so that a group's A tiles stay in L2)
   if (warp == 0) {
     if (lane == 0) {
       uint64_t u = 0;
       bool ok = true;
       for (uint64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        uint64_t mi, nj;
-        kmat_tile(tile, mt, nt, mi, nj);
+        const uint64_t mi = tlist[2 * tile], nj = tlist[2 * tile + 1] & 0x3fffffffu;
         for (uint32_t kb = 0; kb < KB; ++kb, ++u) {
           const uint32_t s = (uint32_t)(u % S), ph = (uint32_t)((u / S) & 1u);
           if (!mbar_wait_bounded(&ts->empty[s], ph ^ 1u, abort_flag, KWAIT_NS)) { fail(1); ok = false; break; }
           mbar_arrive_expect_tx(&ts->full[s], stage_bytes);
           uint8_t* dst = smem + (size_t)s * stage_bytes;
-          tma_load_2d(dst, &tA, (int)(kb * 64), (int)(prow0 + mi * KM_M), &ts->full[s]);
+          tma_load_2d(dst, &tA, (int)(kb * 64), (int)(mi * KM_M), &ts->full[s]);
           tma_load_2d(dst + KA_BYTES, &tB, (int)(kb * 64), (int)(nj * KM_N), &ts->full[s]);
           if (X3) {
-            tma_load_2d(dst + KA_BYTES + KB_BYTES, &tAlo, (int)(kb * 64), (int)(prow0 + mi * KM_M), &ts->full[s]);
+            tma_load_2d(dst + KA_BYTES + KB_BYTES, &tAlo, (int)(kb * 64), (int)(mi * KM_M), &ts->full[s]);
             tma_load_2d(dst + 2 * KA_BYTES + KB_BYTES, &tBlo, (int)(kb * 64), (int)(nj * KM_N), &ts->full[s]);
           }
         }
@@ -303,10 +307,13 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
     uint64_t t = (uint64_t)set;
     for (uint64_t tile = blockIdx.x + (uint64_t)set * gridDim.x; tile < ntiles;
          tile += 2ull * gridDim.x, t += 2) {
-      uint64_t mi, nj;
-      kmat_tile(tile, mt, nt, mi, nj);
-      const uint64_t row = prow0 + mi * KM_M + r, c0 = nj * KM_N;
-      const float ni = (row < prow_end) ? xn2[row] : 0.0f;
+      const uint64_t mi = tlist[2 * tile];
+      const uint32_t njf = tlist[2 * tile + 1];
+      const uint64_t nj = njf & 0x3fffffffu;
+      const bool direct = (njf >> 30) & 1u, mirror = (njf >> 31) & 1u;
+      const uint64_t row = mi * KM_M + r, c0 = nj * KM_N;
+      const bool row_in = row < n;
+      const float ni = row_in ? xn2[row] : 0.0f;
       // column norms only matter for the Gaussian kernel (broadcast loads)
       auto colnorm = [&](uint64_t c) -> float {
         return (KIND == KM_KERNEL_GAUSSIAN && c < n) ? __ldg(xn2 + c) : 0.0f;
@@ -318,11 +325,18 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
       // columns, 16-byte chunks XOR-swizzled by row) and leave as whole
       // 128-byte row segments: eight lanes per row, four rows per store.
       float* stg = stg_all + (size_t)(warp - 4) * 32 * 32;
-      const uint64_t row0 = prow0 + mi * KM_M + (uint64_t)q * 32u;  // first row of this warp
+      const uint64_t row0 = mi * KM_M + (uint64_t)q * 32u;  // first row of this warp
       for (uint32_t pr = 0; pr < KM_N / 64; ++pr) {
         uint32_t acc[64];
         tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
         tmem_ld_wait();
+        if (pr + 1 == KM_N / 64) {
+          // the accumulator's last columns are in registers: the MMAs of the
+          // next tile on this buffer may start while this one is stored
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&ts->tempty[set]);
+        }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const uint64_t cb = c0 + pr * 64u + (uint32_t)h * 32u;
@@ -334,22 +348,37 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
             o.y = kfn_apply_k<KIND>(f, __uint_as_float(acc[h * 32 + 4 * c + 1]), ni, colnorm(cb + 4 * c + 1));
             o.z = kfn_apply_k<KIND>(f, __uint_as_float(acc[h * 32 + 4 * c + 2]), ni, colnorm(cb + 4 * c + 2));
             o.w = kfn_apply_k<KIND>(f, __uint_as_float(acc[h * 32 + 4 * c + 3]), ni, colnorm(cb + 4 * c + 3));
-            if (diag && row < prow_end) {
+            if (diag && direct && row >= prow0 && row < prow_end) {
               if (cb + 4 * c + 0 == row) diag[row] = o.x;
               if (cb + 4 * c + 1 == row) diag[row] = o.y;
               if (cb + 4 * c + 2 == row) diag[row] = o.z;
               if (cb + 4 * c + 3 == row) diag[row] = o.w;
             }
             *reinterpret_cast<float4*>(stg + lane * 32 + ((c ^ (lane & 7)) * 4)) = o;
+            if (mirror && row_in) {
+              // transposed: K[gcol][row]; the warp's lanes write one contiguous run
+              const float ov[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+              for (int qq = 0; qq < 4; ++qq) {
+                const uint64_t gcol = cb + 4 * c + qq;
+                if (gcol >= prow0 && gcol < prow_end) {
+                  if (OUT_BF16)
+                    reinterpret_cast<__nv_bfloat16*>(K)[(gcol - prow0) * n + row] = __float2bfloat16_rn(ov[qq]);
+                  else
+                    reinterpret_cast<float*>(K)[(gcol - prow0) * n + row] = ov[qq];
+                }
+              }
+            }
           }
           __syncwarp();
+          if (!direct) continue;                         // the staged copy is stored only for own rows
 #pragma unroll
           for (int step = 0; step < 8; ++step) {
             const uint32_t rr = (uint32_t)step * 4u + ((uint32_t)lane >> 3);   // row within the warp's 32
             const uint32_t ch = (uint32_t)lane & 7u;                           // 16-byte chunk of the row
             const float4 o = *reinterpret_cast<const float4*>(stg + rr * 32 + ((ch ^ (rr & 7u)) * 4u));
             const uint64_t grow = row0 + rr, gcol = cb + ch * 4u;
-            if (grow >= prow_end) continue;
+            if (grow < prow0 || grow >= prow_end) continue;
             if (OUT_BF16) {
               __nv_bfloat16* Kp = reinterpret_cast<__nv_bfloat16*>(K) + (grow - prow0) * n + gcol;
               if (vec && gcol + 3 < n) {
@@ -378,9 +407,6 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
           }
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&ts->tempty[set]);
     }
   }
   tc_fence_before();
@@ -899,6 +925,53 @@ km_status prepare_kmat_norms(LloydEngine& e, uint64_t n, const KFn& f, int preci
 // the tensor-core precisions it uses the BF16 copies prepared by the engine
 // and the operand norms of prepare_kmat_norms.  skip_done: the launch does
 // nothing once the fit has stopped (panels rebuilt inside the iteration).
+// Tiles of the symmetric tensor-core build of rows [row0, row_end): row tile
+// mi (128 rows) against column block nj (256 columns) for mi / 2 <= nj, in
+// groups of KM_GROUP row tiles with the column blocks inside; `direct` when
+// the tile's rows meet [row0, row_end), `mirror` (strictly above the
+// diagonal blocks) when its transposed rows do.
+std::vector<uint32_t> kmat_tile_list(uint64_t n, uint64_t row0, uint64_t row_end) {
+  const uint64_t mt = (n + KM_M - 1) / KM_M, nt = (n + KM_N - 1) / KM_N;
+  std::vector<uint32_t> t;
+  for (uint64_t g = 0; g < mt; g += KM_GROUP)
+    for (uint64_t nj = 0; nj < nt; ++nj)
+      for (uint64_t mi = g; mi < std::min<uint64_t>(mt, g + KM_GROUP); ++mi) {
+        if (mi / 2 > nj) continue;
+        const bool direct = mi * KM_M < row_end && mi * KM_M + KM_M > row0;
+        const bool mirror = mi / 2 < nj && nj * KM_N < row_end && nj * KM_N + KM_N > row0;
+        if (!direct && !mirror) continue;
+        t.push_back((uint32_t)mi);
+        t.push_back((uint32_t)nj | (direct ? 1u << 30 : 0u) | (mirror ? 1u << 31 : 0u));
+      }
+  return t;
+}
+
+// The device tile list of rows [row0, row_end), built and copied on first use
+// (which must not be inside a stream capture: prepare_kmat_lists covers the
+// panels of a fit before its graph is captured).
+km_status kmat_tiles_dev(LloydEngine& e, uint64_t n, uint64_t row0, uint64_t row_end, const uint32_t** dev,
+                         uint64_t* count) {
+  for (const auto& l : e.kmat_lists)
+    if (l.row0 == row0 && l.row_end == row_end) { *dev = l.dev; *count = l.count; return KM_OK; }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  KM_CUDA_TRY(cudaStreamIsCapturing(e.stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return KM_ERR_STATE;
+  const std::vector<uint32_t> t = kmat_tile_list(n, row0, row_end);
+  KmatTileList l;
+  l.row0 = row0;
+  l.row_end = row_end;
+  l.count = t.size() / 2;
+  if (cudaMalloc(&l.dev, sizeof(uint32_t) * std::max<size_t>(2, t.size())) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return KM_ERR_ALLOC;
+  }
+  e.kmat_lists.push_back(l);
+  KM_CUDA_TRY(cudaMemcpy(l.dev, t.data(), sizeof(uint32_t) * t.size(), cudaMemcpyHostToDevice));
+  *dev = l.dev;
+  *count = l.count;
+  return KM_OK;
+}
+
 km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32_t d, const KFn& f,
                               int precision, bool out_bf16, void* K, float* diag, uint64_t row0,
                               uint64_t row_end, bool skip_done) {
@@ -932,8 +1005,10 @@ km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32
   if (S > 8) S = 8;
   if (S < 2) return KM_ERR_UNSUPPORTED;
   const size_t smem = fixed + S * stage;
-  const uint64_t tiles = ((rows + KM_M - 1) / KM_M) * ((n + KM_N - 1) / KM_N);
-  const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)e.num_sms);
+  const uint32_t* tl = nullptr;
+  uint64_t tiles = 0;
+  KM_TRY(kmat_tiles_dev(e, n, row0, row_end, &tl, &tiles));
+  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(tiles, (uint64_t)e.num_sms));
   const int vec = (n % 4 == 0) && (reinterpret_cast<uintptr_t>(K) % 16 == 0);
 #define KM_LAUNCH_KMAT(X3_, BF_, KIND_)                                                            \
   do {                                                                                             \
@@ -941,7 +1016,7 @@ km_status build_kernel_matrix(LloydEngine& e, const float* X, uint64_t n, uint32
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));     \
     kmat_tc_kernel<X3_, BF_, KIND_><<<grid, 384, smem, s>>>(tA, tAlo, tB, tBlo, e.xn2, n, row0,    \
                                                             row_end, KBn, (uint32_t)S, f, K, diag, \
-                                                            vec, skip_done ? 1 : 0, e.st);         \
+                                                            vec, skip_done ? 1 : 0, e.st, tl, tiles); \
   } while (0)
 #define KM_LAUNCH_KIND(X3_, BF_)                                                                   \
   do {                                                                                             \
@@ -1224,7 +1299,15 @@ km_status km_kkm_set_data(km_kkm* h, const float* X, int on_device) {
   const KFn f = make_kfn(h->p);
   KM_CUDA_TRY(cudaEventRecord(h->ev0, e.stream));
   KM_TRY(prepare_kmat_norms(e, h->p.n, f, h->p.precision));
-  // with panels (or fused), K is built inside every iteration instead
+  // with panels (or fused), K is built inside every iteration instead; the
+  // panels' tile lists are made here, before any iteration is captured
+  if (h->panel && h->p.precision != KM_PREC_FP32) {
+    for (uint64_t r0 = 0; r0 < h->p.n; r0 += h->panel) {
+      const uint32_t* tl = nullptr;
+      uint64_t cnt = 0;
+      KM_TRY(kmat_tiles_dev(e, h->p.n, r0, std::min<uint64_t>(h->p.n, r0 + h->panel), &tl, &cnt));
+    }
+  }
   if (!h->panel && !h->fused)
     KM_TRY(build_kernel_matrix(e, e.X, h->p.n, h->p.d, f, h->p.precision, h->p.k_bf16 != 0, h->K, h->diag, 0,
                                h->p.n, false));

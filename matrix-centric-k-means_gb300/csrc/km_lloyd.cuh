@@ -3,6 +3,8 @@
 #pragma once
 
 #include <cuda.h>
+
+#include <vector>
 #include "km_internal.cuh"
 
 namespace km {
@@ -83,6 +85,13 @@ km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_
                              DevState* st, cudaStream_t s, const uint32_t* order = nullptr);
 
 // ---- engine ----
+// Tile list of one symmetric kernel-matrix build of rows [row0, row_end)
+// (device array of `count` (row tile, column block | flags) pairs).
+struct KmatTileList {
+  uint64_t row0 = 0, row_end = 0, count = 0;
+  uint32_t* dev = nullptr;
+};
+
 struct LloydEngine {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -143,6 +152,7 @@ struct LloydEngine {
   bool a_exact = false;     // every point coordinate is a BF16 value
   CUtensorMap tmA{}, tmAlo{}, tmB{}, tmBlo{};
   bool data_ready = false;
+  std::vector<KmatTileList> kmat_lists;   // symmetric kernel-matrix builds (km_kkm.cu)
 
   ~LloydEngine();
   km_status init(uint64_t n, uint32_t d, uint32_t k, int precision, int device, void* stream,
