@@ -82,19 +82,24 @@ void Kmeans::setup(const float* X, const int* seed, InitMethod initMethod, Kerne
     p.sigma = kp.sigma;
     p.degree = kp.degree;
     p.precision = to_prec(precision, kernel == Kernel::linear);
-    if (precision == Precision::automatic) {
-      // an FP32 n*n kernel matrix that does not fit the device: no stored K
-      // (fused split-BF16x3) instead of rebuilding FP32 panels every iteration
-      uint64_t fr = 0, tot = 0;
-      if (km_mem_info(0, &fr, &tot) == KM_OK && (double)n * (double)n * 4.0 > 0.9 * (double)fr)
-        p.precision = KM_PREC_BF16X3;
-    }
     p.k_bf16 = 0;
     p.check_converged = 0;
     p.device = 0;
     p.stream = nullptr;
     p.panel_rows = KM_KKM_PANEL_AUTO;    // K resident when it fits, else rebuilt in panels
     check(km_kkm_create(&p, &kkm_), "km_kkm_create");
+    if (precision == Precision::automatic && p.precision == KM_PREC_FP32) {
+      // One decision, the handle's own: when it chose panels (the FP32 n*n
+      // kernel matrix does not fit), keep no K at all instead (fused
+      // split-BF16x3) rather than rebuild FP32 panels every iteration.
+      uint64_t rows = 0;
+      if (km_kkm_panel_rows(kkm_, &rows) == KM_OK && rows != 0) {
+        km_kkm_destroy(kkm_);
+        kkm_ = nullptr;
+        p.precision = KM_PREC_BF16X3;
+        check(km_kkm_create(&p, &kkm_), "km_kkm_create");
+      }
+    }
     km_status s = km_kkm_set_data(kkm_, X, 0);
     if (s != KM_OK) {
       km_kkm_destroy(kkm_);
