@@ -25,9 +25,9 @@ static __device__ __forceinline__ float f_inf() { return __int_as_float(0x7f8000
 // Preparation
 // ---------------------------------------------------------------------------
 
-// One warp per row: ||x||^2 (FP64 sum, stored as float and as a per-row double
-// for the deterministic total), non-finite check, and the BF16 hi/lo copies
-// padded with zeros to dp columns (only when Xb != nullptr).
+// One warp per row: ||x||^2 (an FP32 pair, stored as float and as a per-row
+// double for the deterministic total), non-finite check, and the BF16 hi/lo
+// copies padded with zeros to dp columns (only when Xb != nullptr).
 __global__ void prep_points_kernel(const float* __restrict__ X, uint64_t n, uint32_t d, uint32_t dp,
                                    float* __restrict__ xn2, double* __restrict__ xn2d,
                                    __nv_bfloat16* __restrict__ Xb, __nv_bfloat16* __restrict__ Xlo,
@@ -45,10 +45,12 @@ __global__ void prep_points_kernel(const float* __restrict__ X, uint64_t n, uint
     h = t;
     l = __fadd_rn(l, __fadd_rn(al, err));
   };
+  // NaN/Inf and non-BF16 coordinates are flagged once per warp (after its
+  // rows), not once per row: an atomic per row on one word serialises.
+  bool bad = false, inexact = false;
   for (uint64_t r = warp; r < n; r += nw) {
     const float* x = X + r * d;
     float sh = 0.0f, sl = 0.0f;
-    bool bad = false, inexact = false;
     for (uint32_t j = lane; j < dp; j += 32) {
       float v = (j < d) ? x[j] : 0.0f;
       if (!isfinite(v)) bad = true;
@@ -66,13 +68,13 @@ __global__ void prep_points_kernel(const float* __restrict__ X, uint64_t n, uint
       two_sum(sh, sl, oh, ol);
     }
     const double s = (double)sh + (double)sl;
-    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&st->err, KM_DEVERR_NONFINITE);
-    if (__any_sync(0xffffffffu, inexact) && lane == 0) atomicOr(&st->x_not_bf16, 1u);
     if (lane == 0) {
       xn2[r] = (float)s;
       if (xn2d) xn2d[r] = s;
     }
   }
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&st->err, KM_DEVERR_NONFINITE);
+  if (__any_sync(0xffffffffu, inexact) && lane == 0) atomicOr(&st->x_not_bf16, 1u);
 }
 
 // Deterministic FP64 sum: fixed-shape tree per block, block partials summed in
