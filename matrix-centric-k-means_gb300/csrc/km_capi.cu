@@ -341,6 +341,7 @@ km_status km_lloyd_profile(km_lloyd* h, uint64_t iters, double* stage_ms) {
   e.h_st->done = 0;
   e.h_st->iter = 0;
   e.h_st->fin_ticket = 0;
+  e.h_st->scan_ticket = 0;
   KM_CUDA_TRY(cudaMemcpyAsync(e.st, e.h_st, sizeof(DevState), cudaMemcpyHostToDevice, e.stream));
   LoopConsts lc{~0ull, h->p.tol, KM_CONV_NONE, h->p.empty};
   cudaEvent_t ev[6];

@@ -192,6 +192,7 @@ km_status LloydEngine::init(uint64_t n_, uint32_t d_, uint32_t k_, int precision
     KM_CUDA_TRY(cudaFuncSetAttribute(seg_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem));
     KM_CUDA_TRY(cudaFuncSetAttribute(seg_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_smem));
   }
+  KM_TRY(refine_prepare());
   if (need_update) {
     KM_TRY(update_sums_prepare());
     KM_TRY(dalloc(&Cn, (size_t)k * d));
@@ -356,20 +357,22 @@ km_status LloydEngine::enqueue_assign(float* Dout) {
 }
 
 km_status LloydEngine::enqueue_finalize(const LoopConsts& lc) {
-  finalize_kernel<<<(k * 32 + 255) / 256, 256, 0, stream>>>(Cn, C, dsq, objpart, counts, lc.empty, d, dp, k,
-                                                            lc.tol, cn2,
-                                                            Cb, Clo, Ct, shift_c, obj_c, st, lc);
+  KM_CUDA_TRY(launch_pdl(finalize_kernel, (k * 32 + 255) / 256, 256, 0, stream, Cn, C, dsq, objpart, counts,
+                         lc.empty, d, dp, k, lc.tol, cn2, Cb, Clo, Ct, shift_c, obj_c, st, lc));
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }
 
 km_status LloydEngine::enqueue_sort(const uint32_t* lab) {
   const unsigned hb = (nseg + sort_wpb - 1) / sort_wpb;
-  seg_hist_kernel<<<hb, sort_wpb * 32, sort_smem, stream>>>(lab, n, k, seg, nseg, seghist, st);
-  seg_scan_kernel<<<(k * 32 + 255) / 256, 256, 0, stream>>>(seghist, k, nseg, counts, st);
-  cluster_scan_kernel<<<1, 1024, 0, stream>>>(counts, k, cstart, st, k <= 1024u ? order : nullptr);
-  seg_scatter_kernel<<<hb, sort_wpb * 32, sort_smem, stream>>>(lab, n, k, seg, nseg, seghist, cstart,
-                                                               perm, st);
+  // programmatic dependent launches: each kernel waits for its predecessor
+  // (griddepcontrol.wait) before reading, but is scheduled while it drains
+  KM_CUDA_TRY(launch_pdl(seg_hist_kernel, hb, sort_wpb * 32, sort_smem, stream, lab, n, k, seg, nseg, seghist, st));
+  // per-cluster segment scans; the last block also scans the cluster counts
+  KM_CUDA_TRY(launch_pdl(seg_scan_kernel, (k * 32 + 511) / 512, 512, 0, stream, seghist, k, nseg, counts, st,
+                         cstart, k <= 1024u ? order : (uint32_t*)nullptr));
+  KM_CUDA_TRY(launch_pdl(seg_scatter_kernel, hb, sort_wpb * 32, sort_smem, stream, lab, n, k, seg, nseg, seghist,
+                         cstart, perm, st));
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }

@@ -48,7 +48,7 @@ struct DevState {
   unsigned long long refined_total;  // rows re-scored (all iterations)
   unsigned long long full_total;     // of those, against all k centroids
   float cmax;               // max_c ||c|| of the centroids the next assignment uses
-  float pad1;
+  uint32_t scan_ticket;      // seg_scan blocks done in this iteration (the last one resets it)
   double objective;         // FP64 objective of the last assignment
   double last_score;
   double score;
@@ -61,6 +61,29 @@ enum : uint32_t {
   KM_DEVERR_NONFINITE = 2u, // input held NaN/Inf
   KM_DEVERR_OVERFLOW = 4u   // refinement list overflow (cannot happen: list holds n)
 };
+
+// Programmatic dependent launch.  A kernel launched with launch_pdl may be
+// scheduled while its predecessor in the stream is still draining; it calls
+// griddep_wait() before it reads anything the predecessor wrote (the wait
+// returns once the predecessor grid has completed and its writes are
+// visible).  In a kernel launched without the attribute the wait is a no-op.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
 
 // Host mapping of the device error bits to a status (timeouts first).
 inline km_status status_of_device_error(uint32_t err) {
@@ -348,6 +371,12 @@ __device__ __forceinline__ void cp_async16_zfill(void* smem, const void* gmem, u
                "r"(src_bytes)
                : "memory");
 }
+// cp.async groups: close the thread's open group; wait until at most N of its
+// groups are still in flight (the landed copies are visible to this thread;
+// __syncwarp / __syncthreads then orders them for the others).
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 __device__ __forceinline__ void cp_async_mbar_arrive_noinc(uint64_t* bar) {
   asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }

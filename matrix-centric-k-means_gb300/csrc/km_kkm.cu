@@ -326,7 +326,8 @@ kmat_tc_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
       // 128-byte row segments: eight lanes per row, four rows per store.
       float* stg = stg_all + (size_t)(warp - 4) * 32 * 32;
       const uint64_t row0 = mi * KM_M + (uint64_t)q * 32u;  // first row of this warp
-      for (uint32_t pr = 0; pr < KM_N / 64; ++pr) {
+#pragma unroll 1
+      for (uint32_t pr = 0; pr < KM_N / 64; ++pr) {       // not unrolled: the body is large
         uint32_t acc[64];
         tmem_ld_32x32b_x64(tbase + pr * 64u, acc);
         tmem_ld_wait();

@@ -35,8 +35,10 @@ km_status launch_refine_gemm(bool v4, int num_sms, const float* X, const float* 
                              uint32_t* labels, float* mindist, cudaStream_t s);
 __global__ void seg_hist_kernel(const uint32_t* labels, uint64_t n, uint32_t k, uint32_t seg,
                                 uint32_t nseg, uint32_t* seghist, DevState* st);
+// cstart non-null: the block that finishes last also runs cluster_scan_kernel's
+// work (at most 512 threads per block).
 __global__ void seg_scan_kernel(uint32_t* seghist, uint32_t k, uint32_t nseg, uint32_t* counts,
-                                DevState* st);
+                                DevState* st, uint32_t* cstart, uint32_t* order);
 // order (nullable, k <= 1024): clusters by descending count, ties by index.
 __global__ void cluster_scan_kernel(const uint32_t* counts, uint32_t k, uint32_t* cstart,
                                     DevState* st, uint32_t* order);
@@ -79,6 +81,8 @@ km_status launch_assign_tc(const TcPlan& pl, int mode, const CUtensorMap& tmA,
                            float* Dout, cudaStream_t s);
 
 km_status update_sums_prepare();
+// Shared-memory limits of the staged re-score kernels (once per process and device).
+km_status refine_prepare();
 // order (nullable): the clusters' processing order (largest first).
 km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_t* cstart, uint32_t d,
                              uint32_t k, const float* C, float* Cn, float* dsq, double* objpart,

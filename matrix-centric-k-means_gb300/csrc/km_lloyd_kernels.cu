@@ -161,6 +161,7 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
                   uint32_t* __restrict__ labels, float* __restrict__ mindist,
                   RefineQueues rq, float* __restrict__ Dout, const uint32_t* __restrict__ ridx,
                   const uint32_t* __restrict__ nidx) {
+  griddep_wait();
   if (st->done) return;
   // Gather mode (ridx != null): logical row li of the tiles is row ridx[li] of X,
   // for li < *nidx; queue segments are taken over the logical rows.
@@ -352,6 +353,7 @@ __global__ void __launch_bounds__(32 * RC_WARPS)
 refine_cands_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
                     DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
                     float* __restrict__ mindist, bool count) {
+  griddep_wait();
   if (st->done) return;
   __shared__ uint32_t block_rows;
   if (threadIdx.x == 0) block_rows = 0;
@@ -450,211 +452,115 @@ __device__ __forceinline__ float cpu_dist_v4(const float* __restrict__ x, const 
   return s;
 }
 
-// The same re-score with the (row, candidate) pairs packed one per lane
-// (d % 4 == 0, 16-byte aligned rows): a warp takes RP_SEGS queue segments,
-// lane e loads entry e, a warp prefix over the candidate counts places pair
-// (e, m) on lane off[e] + m, every lane runs one exact chain, and lane e picks
-// its row's minimum (candidates are in ascending index order, so a strict '<'
-// keeps the lowest index on ties).  With 2..4 candidates per row and a few
-// rows per segment, four lanes per row left most lanes idle.
-constexpr int RP_SEGS = 4;
-
-__global__ void __launch_bounds__(32 * RC_WARPS, 2)
-refine_pairs_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
-                    DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
-                    float* __restrict__ mindist, bool count) {
-  if (st->done) return;
-  __shared__ float sv[RC_WARPS][32][4];
-  __shared__ uint32_t block_rows;
-  if (threadIdx.x == 0) block_rows = 0;
-  __syncthreads();
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t seg0 = warp * RP_SEGS;
-  const uint32_t c = (lane < RP_SEGS && seg0 + (uint64_t)lane < rq.nseg) ? rq.ccnt[seg0 + lane] : 0u;
-  uint32_t pre[RP_SEGS];
-  uint32_t run = 0;
-#pragma unroll
-  for (int q = 0; q < RP_SEGS; ++q) {
-    run += __shfl_sync(0xffffffffu, c, q);
-    pre[q] = run;
-  }
-  const uint32_t total = run;
-  for (uint32_t e0 = 0; e0 < total; e0 += 32) {
-    const uint32_t qi = e0 + (uint32_t)lane;
-    const bool has = qi < total;
-    RefineEntry en{0u, 0u, {0u, 0u, 0u, 0u}};
-    if (has) {
-      uint32_t sg = 0, before = 0;
-#pragma unroll
-      for (int q = 0; q < RP_SEGS - 1; ++q)
-        if (qi >= pre[q]) { sg = (uint32_t)q + 1u; before = pre[q]; }
-      en = rq.cand[(seg0 + sg) * 32 + (qi - before)];
-    }
-    const uint32_t cl = has ? min(en.cnt, 4u) : 0u;
-    // exclusive prefix of the candidate counts over the lanes
-    uint32_t incl = cl;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const uint32_t off = incl - cl;
-    const uint32_t npairs = __shfl_sync(0xffffffffu, incl, 31);
-    for (uint32_t p0 = 0; p0 < npairs; p0 += 32) {
-      const uint32_t p = p0 + (uint32_t)lane;
-      // owner: the last lane whose offset is <= p
-      uint32_t e = 0;
-#pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        const uint32_t cand = e + (uint32_t)step;
-        const uint32_t oc = __shfl_sync(0xffffffffu, off, (int)(cand & 31u));
-        if (cand < 32u && oc <= p) e = cand;
-      }
-      const uint32_t m = p - __shfl_sync(0xffffffffu, off, (int)e);
-      const uint32_t row = __shfl_sync(0xffffffffu, en.row, (int)e);
-      const uint32_t c0 = __shfl_sync(0xffffffffu, en.c[0], (int)e);
-      const uint32_t c1 = __shfl_sync(0xffffffffu, en.c[1], (int)e);
-      const uint32_t c2 = __shfl_sync(0xffffffffu, en.c[2], (int)e);
-      const uint32_t c3 = __shfl_sync(0xffffffffu, en.c[3], (int)e);
-      if (p < npairs) {
-        const uint32_t cc = m == 0 ? c0 : m == 1 ? c1 : m == 2 ? c2 : c3;
-        sv[wib][e][m & 3u] = cpu_dist_v4(X + (uint64_t)row * d, C + (uint64_t)cc * d, d);
-      }
-    }
-    __syncwarp();
-    if (has) {
-      float bv = sv[wib][lane][0];
-      uint32_t bi = en.c[0];
-#pragma unroll
-      for (uint32_t m = 1; m < 4; ++m)
-        if (m < cl && sv[wib][lane][m] < bv) { bv = sv[wib][lane][m]; bi = en.c[m]; }
-      labels[en.row] = bi;
-      if (mindist) mindist[en.row] = bv;
-    }
-    __syncwarp();
-  }
-  if (count && lane == 0 && total) atomicAdd(&block_rows, total);
-  __syncthreads();
-  if (count && threadIdx.x == 0 && block_rows)
-    atomicAdd(&st->refined_total, (unsigned long long)block_rows);
-}
-
-static void launch_refine_cands(bool v4, const float* X, const float* C, uint32_t d, DevState* st,
-                                const RefineQueues& rq, uint32_t* labels, float* mindist, bool count,
-                                cudaStream_t s) {
-  if (v4) {
-    const uint64_t warps = (rq.nseg + RP_SEGS - 1) / RP_SEGS;
-    const unsigned blocks = (unsigned)std::max<uint64_t>(1, (warps + RC_WARPS - 1) / RC_WARPS);
-    refine_pairs_kernel<<<blocks, 32 * RC_WARPS, 0, s>>>(X, C, d, st, rq, labels, mindist, count);
-  } else {
-    const uint64_t warps = (rq.nseg + RC_SEGS - 1) / RC_SEGS;
-    const unsigned blocks = (unsigned)std::max<uint64_t>(1, (warps + RC_WARPS - 1) / RC_WARPS);
-    refine_cands_kernel<<<blocks, 32 * RC_WARPS, 0, s>>>(X, C, d, st, rq, labels, mindist, count);
-  }
-}
-
-// Exact re-score against all k centroids: one warp per group of up to four
-// rows of a segment, lanes over centroids (eight chains per lane and row),
-// centroids read from the transposed copy Ct (d x k) so that every load of
-// the warp is one coalesced 128-byte line and serves all rows of the group.
-// Per lane the centroids are visited in ascending order with a strict '<'
-// and the warp reduction keeps the lowest index on ties: the reference's
-// argmin (kmeans.cpp:106-122).
+// Exact re-score of a group of up to FULL_ROWS rows (row ids rows[0..nr))
+// against all k centroids by one warp: lanes over centroids (eight chains per
+// lane and row), centroids read from the transposed copy Ct (d x k) so that
+// every load of the warp is one coalesced 128-byte line and serves all rows of
+// the group.  Per lane the centroids are visited in ascending order with a
+// strict '<' and the warp reduction keeps the lowest index on ties: the
+// reference's argmin (kmeans.cpp:106-122).
 constexpr int FULL_ROWS = 4;
 
+__device__ __forceinline__ void full_rescore_group(const float* __restrict__ X, const float* __restrict__ Ct,
+                                                   uint32_t d, uint32_t k, const uint32_t* rows, uint32_t nr,
+                                                   uint32_t* __restrict__ labels, float* __restrict__ mindist) {
+  const int lane = threadIdx.x & 31;
+  uint32_t row[FULL_ROWS];
+  const float* x[FULL_ROWS];
+#pragma unroll
+  for (int r = 0; r < FULL_ROWS; ++r) {
+    row[r] = rows[min((uint32_t)r, nr - 1)];   // pad with the last row
+    x[r] = X + (uint64_t)row[r] * d;
+  }
+  float bv[FULL_ROWS];
+  uint32_t bi[FULL_ROWS];
+#pragma unroll
+  for (int r = 0; r < FULL_ROWS; ++r) { bv[r] = f_inf(); bi[r] = 0xffffffffu; }
+  for (uint32_t cb = 0; cb < k; cb += 256) {
+    float s[FULL_ROWS][8];
+#pragma unroll
+    for (int r = 0; r < FULL_ROWS; ++r)
+#pragma unroll
+      for (int t = 0; t < 8; ++t) s[r][t] = 0.0f;
+    // Four j steps per group: all their loads (the rows' x_j, the lanes'
+    // centroid columns from Ct) are issued before the group's arithmetic,
+    // which keeps 48 loads in flight per lane instead of one step's.
+    for (uint32_t j0 = 0; j0 < d; j0 += 4) {
+      float xj[4][FULL_ROWS], cv[4][8];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t j = j0 + (uint32_t)q;
+        const bool jin = j < d;
+#pragma unroll
+        for (int r = 0; r < FULL_ROWS; ++r) xj[q][r] = jin ? x[r][j] : 0.0f;
+        const float* ct = Ct + (uint64_t)(jin ? j : 0u) * k + cb + lane;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) cv[q][t] = (jin && cb + lane + 32 * t < k) ? ct[32 * t] : 0.0f;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (j0 + (uint32_t)q >= d) break;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+#pragma unroll
+          for (int r = 0; r < FULL_ROWS; ++r) {
+            const float tt = __fsub_rn(xj[q][r], cv[q][t]);
+            s[r][t] = __fadd_rn(s[r][t], __fmul_rn(tt, tt));
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const uint32_t c = cb + lane + 32 * t;
+#pragma unroll
+      for (int r = 0; r < FULL_ROWS; ++r)
+        if (c < k && s[r][t] < bv[r]) { bv[r] = s[r][t]; bi[r] = c; }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < FULL_ROWS; ++r) {
+    float v = bv[r];
+    uint32_t i = bi[r];
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+      const uint32_t oi = __shfl_xor_sync(0xffffffffu, i, o);
+      if (ov < v || (ov == v && oi < i)) { v = ov; i = oi; }
+    }
+    if (lane == 0 && (uint32_t)r < nr) {
+      labels[row[r]] = (i == 0xffffffffu) ? 0u : i;
+      if (mindist) mindist[row[r]] = v;
+    }
+  }
+}
+
+// Rows of the full queue, warp by warp: segments warp, warp + nw, warp + 2 nw,
+// ... (a dense queue spreads over all warps); 32 of their counts per load,
+// only the non-empty ones visited.
 __global__ void __launch_bounds__(256, 2)
 refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, uint32_t d, uint32_t k,
                    DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
                    float* __restrict__ mindist, bool count) {
+  griddep_wait();
   if (st->done) return;
   const int lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   uint32_t done_rows = 0;
-  // Segments warp, warp + nw, warp + 2 nw, ... (a dense queue spreads over all
-  // warps); 32 of their counts per load, only the non-empty ones visited.
   for (uint64_t g0 = warp; g0 < rq.nseg; g0 += nw * 32) {
-   const uint64_t sgl = g0 + (uint64_t)lane * nw;
-   const uint32_t cl = (sgl < rq.nseg) ? rq.fcnt[sgl] : 0u;
-   uint32_t nz = __ballot_sync(0xffffffffu, cl != 0u);
-   while (nz) {
-   const int sl = __ffs(nz) - 1;
-   nz &= nz - 1u;
-   const uint64_t seg = g0 + (uint64_t)sl * nw;
-   const uint32_t cnt = __shfl_sync(0xffffffffu, cl, sl);
-   done_rows += cnt;
-   for (uint32_t e0 = 0; e0 < cnt; e0 += FULL_ROWS) {
-    const uint32_t nr = min(cnt - e0, (uint32_t)FULL_ROWS);
-    uint32_t row[FULL_ROWS];
-    const float* x[FULL_ROWS];
-#pragma unroll
-    for (int r = 0; r < FULL_ROWS; ++r) {
-      row[r] = rq.full[seg * 32 + e0 + min((uint32_t)r, nr - 1)];   // pad with the last row
-      x[r] = X + (uint64_t)row[r] * d;
+    const uint64_t sgl = g0 + (uint64_t)lane * nw;
+    const uint32_t cl = (sgl < rq.nseg) ? rq.fcnt[sgl] : 0u;
+    uint32_t nz = __ballot_sync(0xffffffffu, cl != 0u);
+    while (nz) {
+      const int sl = __ffs(nz) - 1;
+      nz &= nz - 1u;
+      const uint64_t seg = g0 + (uint64_t)sl * nw;
+      const uint32_t cnt = __shfl_sync(0xffffffffu, cl, sl);
+      done_rows += cnt;
+      for (uint32_t e0 = 0; e0 < cnt; e0 += FULL_ROWS)
+        full_rescore_group(X, Ct, d, k, rq.full + seg * 32 + e0, min(cnt - e0, (uint32_t)FULL_ROWS), labels,
+                           mindist);
     }
-    float bv[FULL_ROWS];
-    uint32_t bi[FULL_ROWS];
-#pragma unroll
-    for (int r = 0; r < FULL_ROWS; ++r) { bv[r] = f_inf(); bi[r] = 0xffffffffu; }
-    for (uint32_t cb = 0; cb < k; cb += 256) {
-      float s[FULL_ROWS][8];
-#pragma unroll
-      for (int r = 0; r < FULL_ROWS; ++r)
-#pragma unroll
-        for (int t = 0; t < 8; ++t) s[r][t] = 0.0f;
-      // Four j steps per group: all their loads (the rows' x_j, the lanes'
-      // centroid columns from Ct) are issued before the group's arithmetic,
-      // which keeps 48 loads in flight per lane instead of one step's.
-      for (uint32_t j0 = 0; j0 < d; j0 += 4) {
-        float xj[4][FULL_ROWS], cv[4][8];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint32_t j = j0 + (uint32_t)q;
-          const bool jin = j < d;
-#pragma unroll
-          for (int r = 0; r < FULL_ROWS; ++r) xj[q][r] = jin ? x[r][j] : 0.0f;
-          const float* ct = Ct + (uint64_t)(jin ? j : 0u) * k + cb + lane;
-#pragma unroll
-          for (int t = 0; t < 8; ++t) cv[q][t] = (jin && cb + lane + 32 * t < k) ? ct[32 * t] : 0.0f;
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          if (j0 + (uint32_t)q >= d) break;
-#pragma unroll
-          for (int t = 0; t < 8; ++t) {
-#pragma unroll
-            for (int r = 0; r < FULL_ROWS; ++r) {
-              const float tt = __fsub_rn(xj[q][r], cv[q][t]);
-              s[r][t] = __fadd_rn(s[r][t], __fmul_rn(tt, tt));
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        const uint32_t c = cb + lane + 32 * t;
-#pragma unroll
-        for (int r = 0; r < FULL_ROWS; ++r)
-          if (c < k && s[r][t] < bv[r]) { bv[r] = s[r][t]; bi[r] = c; }
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < FULL_ROWS; ++r) {
-      float v = bv[r];
-      uint32_t i = bi[r];
-      for (int o = 16; o > 0; o >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, v, o);
-        const uint32_t oi = __shfl_xor_sync(0xffffffffu, i, o);
-        if (ov < v || (ov == v && oi < i)) { v = ov; i = oi; }
-      }
-      if (lane == 0 && (uint32_t)r < nr) {
-        labels[row[r]] = (i == 0xffffffffu) ? 0u : i;
-        if (mindist) mindist[row[r]] = v;
-      }
-    }
-   }
-   }
   }
   if (count && lane == 0 && done_rows) {
     atomicAdd(&st->refined_total, (unsigned long long)done_rows);
@@ -662,10 +568,214 @@ refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, ui
   }
 }
 
+// Exact re-score of the candidate queue with its operands staged in shared
+// memory (d % 4 == 0, 16-byte aligned rows).  Each warp owns ranges of `span`
+// (<= 32) consecutive queue segments, one segment count per lane, and walks a
+// range's entries in passes.  A pass takes the leading entries whose point
+// rows and candidate centroid rows fit RS_ROWS staged rows: the entries' point
+// rows at [0, ne), the pairs' centroid rows at [ne, ne + np), pair p on lane p.
+// The rows are copied by 16-byte cp.async, one row per instruction on
+// contiguous lanes (four 128-byte lines), RS_CH columns per round trip (all of
+// d when d <= RS_CH); the loads of the next pass's entries are issued before
+// the copies are waited on.  Every lane then runs the reference's ordered
+// chain (float, j ascending, no contraction) from shared memory.  A lane that
+// loads its own rows straight from global memory touches up to 32 lines per
+// instruction, and the L1 wavefronts, not DRAM, then set the time.  The
+// entry's lane picks the smallest distance over its candidates in ascending
+// index order with a strict '<' (lowest index on ties).  The candidate set
+// provably holds the reference argmin over all k (tie_tau / tie_class).
+// FULL: the warp also re-scores the rows of its segments' full queue against
+// all k (full_rescore_group), so that one launch covers the whole refinement.
+constexpr int RS_WARPS = 4;
+constexpr int RS_ROWS = 32;              // staged rows per pass
+constexpr uint32_t RS_CH = 128;          // staged columns per round trip
+constexpr int RS_BLOCKS_PER_SM = 3;
+// Shared row stride in floats for chunks of ch columns, with (stride / 4) odd
+// so that float4 reads of eight consecutive rows cover the 32 banks.
+__host__ __device__ constexpr uint32_t rs_ld(uint32_t ch) { return ((ch + 4u) / 4u) % 2u ? ch + 4u : ch + 8u; }
+constexpr size_t RS_SMEM_MAX = (size_t)RS_WARPS * RS_ROWS * rs_ld(RS_CH) * sizeof(float);
+
+template <bool FULL>
+__global__ void __launch_bounds__(32 * RS_WARPS, RS_BLOCKS_PER_SM)
+refine_staged_kernel(const float* __restrict__ X, const float* __restrict__ C, const float* __restrict__ Ct,
+                     uint32_t d, uint32_t k, uint32_t span, DevState* st, RefineQueues rq,
+                     uint32_t* __restrict__ labels, float* __restrict__ mindist, bool count) {
+  griddep_wait();
+  if (st->done) return;
+  extern __shared__ __align__(16) float rs_smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const uint32_t ch = min(d, RS_CH), ld = rs_ld(ch);
+  float* const stg = rs_smem + (size_t)wib * RS_ROWS * ld;
+  const uint64_t nranges = (rq.nseg + span - 1) / span;
+  const uint64_t nw = (uint64_t)gridDim.x * RS_WARPS;
+  uint32_t cand_rows = 0, full_rows = 0;
+  for (uint64_t rg = (uint64_t)blockIdx.x * RS_WARPS + wib; rg < nranges; rg += nw) {
+    const uint64_t seg0 = rg * span;
+    const bool segok = (uint32_t)lane < span && seg0 + (uint64_t)lane < rq.nseg;
+    const uint32_t c = segok ? rq.ccnt[seg0 + lane] : 0u;
+    const uint32_t fc = (FULL && segok) ? rq.fcnt[seg0 + lane] : 0u;
+    uint32_t pre = c;   // inclusive prefix of the segment counts over the lanes
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, pre, o);
+      if (lane >= o) pre += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
+    cand_rows += total;
+    // Entry t of the range (all lanes call; loads only for t < total): its
+    // segment is the number of lanes whose prefix is <= t.
+    auto load_entry = [&](uint32_t t) {
+      uint32_t sg = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const uint32_t pv = __shfl_sync(0xffffffffu, pre, (int)(sg + (uint32_t)step - 1u));
+        if (pv <= t) sg += (uint32_t)step;
+      }
+      const uint32_t before = __shfl_sync(0xffffffffu, pre, (int)((sg + 31u) & 31u));
+      RefineEntry r{0u, 0u, {0u, 0u, 0u, 0u}};
+      if (t < total) r = rq.cand[(seg0 + sg) * 32 + (t - (sg ? before : 0u))];
+      return r;
+    };
+    RefineEntry en = load_entry((uint32_t)lane);
+    for (uint32_t e0 = 0; e0 < total;) {
+      const bool has = e0 + (uint32_t)lane < total;
+      const uint32_t cl = has ? max(1u, min(en.cnt, 4u)) : 0u;
+      uint32_t incl = cl;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      // entries of this pass: the leading lanes whose rows (one point row per
+      // entry, one centroid row per pair) fit RS_ROWS (at least six, cl <= 4)
+      const uint32_t ne =
+          (uint32_t)__popc(__ballot_sync(0xffffffffu, has && (uint32_t)lane + 1u + incl <= (uint32_t)RS_ROWS));
+      const uint32_t np = __shfl_sync(0xffffffffu, incl, (int)ne - 1);
+      const uint32_t off = incl - cl;
+      // pair p = lane: its entry e (the last entry lane with off <= p)
+      const uint32_t p = (uint32_t)lane;
+      uint32_t e = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const uint32_t t = e + (uint32_t)step;
+        const uint32_t ot = __shfl_sync(0xffffffffu, off, (int)(t & 31u));
+        if (t < ne && ot <= p) e = t;
+      }
+      const uint32_t m = p - __shfl_sync(0xffffffffu, off, (int)e);
+      const uint32_t q0 = __shfl_sync(0xffffffffu, en.c[0], (int)e);
+      const uint32_t q1 = __shfl_sync(0xffffffffu, en.c[1], (int)e);
+      const uint32_t q2 = __shfl_sync(0xffffffffu, en.c[2], (int)e);
+      const uint32_t q3 = __shfl_sync(0xffffffffu, en.c[3], (int)e);
+      const uint32_t cand = m == 0 ? q0 : m == 1 ? q1 : m == 2 ? q2 : q3;   // meaningful for p < np
+      const uint32_t nrows = ne + np;
+      // columns [j0, j0 + nc) of the pass's rows, one row per instruction
+      auto stage = [&](uint32_t j0) {
+        const uint32_t nc4 = min(ch, d - j0) / 4u;
+        for (uint32_t r = 0; r < nrows; ++r) {
+          const uint32_t xr = __shfl_sync(0xffffffffu, en.row, (int)(r & 31u));
+          const uint32_t cr = __shfl_sync(0xffffffffu, cand, (int)((r - ne) & 31u));
+          const float* src = r < ne ? X + (uint64_t)xr * d : C + (uint64_t)cr * d;
+          if ((uint32_t)lane < nc4) cp_async16_zfill(stg + r * ld + 4u * lane, src + j0 + 4u * lane, 16u);
+        }
+        cp_async_commit();
+      };
+      stage(0);
+      const uint32_t e0n = e0 + ne;
+      const RefineEntry enn = load_entry(e0n + (uint32_t)lane);   // in flight during this pass
+      float s = 0.0f;
+      auto step4 = [&](const float4 a, const float4 b) {
+        float t = __fsub_rn(a.x, b.x); s = __fadd_rn(s, __fmul_rn(t, t));
+        t = __fsub_rn(a.y, b.y); s = __fadd_rn(s, __fmul_rn(t, t));
+        t = __fsub_rn(a.z, b.z); s = __fadd_rn(s, __fmul_rn(t, t));
+        t = __fsub_rn(a.w, b.w); s = __fadd_rn(s, __fmul_rn(t, t));
+      };
+      for (uint32_t j0 = 0; j0 < d; j0 += ch) {
+        if (j0) stage(j0);
+        cp_async_wait<0>();
+        __syncwarp();
+        if (p < np) {
+          const float4* xs = reinterpret_cast<const float4*>(stg + e * ld);
+          const float4* cs = reinterpret_cast<const float4*>(stg + (ne + p) * ld);
+          const uint32_t nc4 = min(ch, d - j0) / 4u;
+          if (nc4 == RS_CH / 4u) {
+#pragma unroll 8
+            for (uint32_t q = 0; q < RS_CH / 4u; ++q) step4(xs[q], cs[q]);
+          } else {
+            for (uint32_t q = 0; q < nc4; ++q) step4(xs[q], cs[q]);
+          }
+        }
+        __syncwarp();   // the rows are restaged only after every lane's chain
+      }
+      // entry lane: the smallest of its cl candidates (pairs off .. off+cl-1)
+      float bv = 0.0f;
+      uint32_t bi = 0u;
+#pragma unroll
+      for (uint32_t mm = 0; mm < 4; ++mm) {
+        const int src = (int)((off + mm) & 31u);
+        const float v = __shfl_sync(0xffffffffu, s, src);
+        const uint32_t ci = __shfl_sync(0xffffffffu, cand, src);
+        if (mm == 0 || (mm < cl && v < bv)) { bv = v; bi = ci; }
+      }
+      if ((uint32_t)lane < ne) {
+        labels[en.row] = bi;
+        if (mindist) mindist[en.row] = bv;
+      }
+      en = enn;
+      e0 = e0n;
+    }
+    if (FULL) {
+      for (uint32_t q = 0; q < span; ++q) {
+        const uint32_t cnt = __shfl_sync(0xffffffffu, fc, (int)q);
+        full_rows += cnt;
+        for (uint32_t f0 = 0; f0 < cnt; f0 += FULL_ROWS)
+          full_rescore_group(X, Ct, d, k, rq.full + (seg0 + (uint64_t)q) * 32 + f0,
+                             min(cnt - f0, (uint32_t)FULL_ROWS), labels, mindist);
+      }
+    }
+  }
+  if (count && lane == 0 && cand_rows + full_rows)
+    atomicAdd(&st->refined_total, (unsigned long long)(cand_rows + full_rows));
+  if (count && lane == 0 && full_rows) atomicAdd(&st->full_total, (unsigned long long)full_rows);
+}
+
+// Launch shape of refine_staged_kernel: a persistent grid, each warp a range
+// of `span` consecutive segments.
+struct StagedShape {
+  unsigned blocks;
+  uint32_t span;
+  size_t smem;
+};
+static StagedShape staged_shape(int num_sms, uint64_t nseg, uint32_t d) {
+  const uint64_t max_warps = (uint64_t)num_sms * RS_BLOCKS_PER_SM * RS_WARPS;
+  const uint32_t span = (uint32_t)std::min<uint64_t>(32, std::max<uint64_t>(1, (nseg + max_warps - 1) / max_warps));
+  const uint64_t ranges = (nseg + span - 1) / span;
+  StagedShape sh;
+  sh.blocks = (unsigned)std::max<uint64_t>(
+      1, std::min<uint64_t>((uint64_t)num_sms * RS_BLOCKS_PER_SM, (ranges + RS_WARPS - 1) / RS_WARPS));
+  sh.span = span;
+  sh.smem = (size_t)RS_WARPS * RS_ROWS * rs_ld(std::min<uint32_t>(d, RS_CH)) * sizeof(float);
+  return sh;
+}
+
+static void launch_refine_cands(bool v4, int num_sms, const float* X, const float* C, uint32_t d,
+                                DevState* st, const RefineQueues& rq, uint32_t* labels, float* mindist,
+                                bool count, cudaStream_t s) {
+  if (v4) {
+    const StagedShape sh = staged_shape(num_sms, rq.nseg, d);
+    (void)launch_pdl(refine_staged_kernel<false>, sh.blocks, 32 * RS_WARPS, sh.smem, s, X, C,
+                     (const float*)nullptr, d, 0u, sh.span, st, rq, labels, mindist, count);
+  } else {
+    const uint64_t warps = (rq.nseg + RC_SEGS - 1) / RC_SEGS;
+    const unsigned blocks = (unsigned)std::max<uint64_t>(1, (warps + RC_WARPS - 1) / RC_WARPS);
+    (void)launch_pdl(refine_cands_kernel, blocks, 32 * RC_WARPS, 0, s, X, C, d, st, rq, labels, mindist, count);
+  }
+}
+
 // Rows of the full queue gathered into one list (order irrelevant: every row
 // is re-scored on its own), counted as fully re-scored rows.
 __global__ void full_compact_kernel(DevState* st, RefineQueues rq, uint32_t* __restrict__ out,
                                     uint32_t* __restrict__ nout) {
+  griddep_wait();
   if (st->done) return;
   const int lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -694,6 +804,7 @@ __global__ void __launch_bounds__(256, 2)
 refine_wide_kernel(const float* __restrict__ X, const float* __restrict__ C, uint32_t d,
                    DevState* st, RefineQueues rq, uint32_t* __restrict__ labels,
                    float* __restrict__ mindist) {
+  griddep_wait();
   if (st->done) return;
   const int lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -728,17 +839,31 @@ refine_wide_kernel(const float* __restrict__ X, const float* __restrict__ C, uin
   if (lane == 0 && done_rows) atomicAdd(&st->refined_total, (unsigned long long)done_rows);
 }
 
+km_status refine_prepare() {
+  KM_CUDA_TRY(cudaFuncSetAttribute(refine_staged_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)RS_SMEM_MAX));
+  KM_CUDA_TRY(cudaFuncSetAttribute(refine_staged_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)RS_SMEM_MAX));
+  return KM_OK;
+}
+
 km_status launch_refine(bool v4, int num_sms, const float* X, const float* C, const float* Ct,
                         uint32_t d, uint32_t k, DevState* st, const RefineQueues& rq,
                         uint32_t* labels, float* mindist, cudaStream_t s) {
-  launch_refine_cands(v4, X, C, d, st, rq, labels, mindist, true, s);
-  if (rq.wide) {
-    if (v4)
-      refine_wide_kernel<true><<<num_sms * 8, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
-    else
-      refine_wide_kernel<false><<<num_sms * 8, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
+  // Every row sits in one queue at most, so the queues are re-scored in any order.
+  if (v4) {
+    // candidate and full queues in one launch
+    const StagedShape sh = staged_shape(num_sms, rq.nseg, d);
+    KM_CUDA_TRY(launch_pdl(refine_staged_kernel<true>, sh.blocks, 32 * RS_WARPS, sh.smem, s, X, C, Ct, d, k,
+                           sh.span, st, rq, labels, mindist, true));
+    if (rq.wide)
+      KM_CUDA_TRY(launch_pdl(refine_wide_kernel<true>, num_sms * 8, 256, 0, s, X, C, d, st, rq, labels, mindist));
+  } else {
+    launch_refine_cands(false, num_sms, X, C, d, st, rq, labels, mindist, true, s);
+    if (rq.wide)
+      KM_CUDA_TRY(launch_pdl(refine_wide_kernel<false>, num_sms * 8, 256, 0, s, X, C, d, st, rq, labels, mindist));
+    KM_CUDA_TRY(launch_pdl(refine_full_kernel, num_sms * 4, 256, 0, s, X, Ct, d, k, st, rq, labels, mindist, true));
   }
-  refine_full_kernel<<<num_sms * 4, 256, 0, s>>>(X, Ct, d, k, st, rq, labels, mindist, true);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }
@@ -748,7 +873,7 @@ km_status launch_refine_gemm(bool v4, int num_sms, const float* X, const float* 
                              TieBound tb32, DevState* st, const RefineQueues& rq,
                              const RefineQueues& rq2, uint32_t* fidx, uint32_t* nfull,
                              uint32_t* labels, float* mindist, cudaStream_t s) {
-  launch_refine_cands(v4, X, C, d, st, rq, labels, mindist, true, s);
+  launch_refine_cands(v4, num_sms, X, C, d, st, rq, labels, mindist, true, s);
   if (rq.wide) {
     if (v4)
       refine_wide_kernel<true><<<num_sms * 8, 256, 0, s>>>(X, C, d, st, rq, labels, mindist);
@@ -771,7 +896,7 @@ km_status launch_refine_gemm(bool v4, int num_sms, const float* X, const float* 
   else
     assign_f32_kernel<false><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
                                                     rq2, nullptr, fidx, nfull);
-  launch_refine_cands(v4, X, C, d, st, rq2, labels, mindist, false, s);
+  launch_refine_cands(v4, num_sms, X, C, d, st, rq2, labels, mindist, false, s);
   refine_full_kernel<<<num_sms * 4, 256, 0, s>>>(X, Ct, d, k, st, rq2, labels, mindist, false);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
@@ -785,6 +910,7 @@ km_status launch_refine_gemm(bool v4, int num_sms, const float* X, const float* 
 __global__ void seg_hist_kernel(const uint32_t* __restrict__ labels, uint64_t n, uint32_t k,
                                 uint32_t seg, uint32_t nseg, uint32_t* __restrict__ seghist,
                                 DevState* st) {
+  griddep_wait();
   if (st->done) return;
   extern __shared__ uint32_t sh_cnt[];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -816,51 +942,15 @@ __global__ void seg_hist_kernel(const uint32_t* __restrict__ labels, uint64_t n,
   }
 }
 
-// One warp per cluster: exclusive scan over its segments, total -> counts.
-__global__ void seg_scan_kernel(uint32_t* __restrict__ seghist, uint32_t k, uint32_t nseg,
-                                uint32_t* __restrict__ counts, DevState* st) {
-  if (st->done) return;
-  const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (c >= k) return;
-  uint32_t* h = seghist + (uint64_t)c * nseg;
-  uint32_t carry = 0;
-  // groups of 32 coalesced chunks: every load of a group is issued before the
-  // scans that use them
-  for (uint32_t g = 0; g < nseg; g += 32u * 32u) {
-    uint32_t v[32];
-#pragma unroll
-    for (int q = 0; q < 32; ++q) {
-      const uint32_t i = g + (uint32_t)q * 32u + (uint32_t)lane;
-      v[q] = (i < nseg) ? h[i] : 0u;
-    }
-#pragma unroll
-    for (int q = 0; q < 32; ++q) {
-      const uint32_t i = g + (uint32_t)q * 32u + (uint32_t)lane;
-      uint32_t x = v[q];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-      }
-      if (i < nseg) h[i] = carry + x - v[q];
-      carry += __shfl_sync(0xffffffffu, x, 31);
-    }
-  }
-  if (lane == 0) counts[c] = carry;
-}
-
-// Single block: exclusive scan of the k counts -> cstart[0..k] (CSR row
-// pointers of V).
-__global__ void cluster_scan_kernel(const uint32_t* __restrict__ counts, uint32_t k,
-                                    uint32_t* __restrict__ cstart, DevState* st,
-                                    uint32_t* __restrict__ order) {
-  if (st->done) return;
-  __shared__ uint32_t part[1024];
-  __shared__ uint32_t scnt[1024];
+// Exclusive scan of the k counts -> cstart[0..k] (CSR row pointers of V) by one
+// block (any size up to 1024 threads); order (nullable, k <= 1024): clusters by
+// descending count, ties by index.  Counts are read from L2 (other blocks may
+// have written them in the same launch).
+__device__ void cluster_scan_block(const uint32_t* counts, uint32_t k, uint32_t* __restrict__ cstart,
+                                   uint32_t* __restrict__ order, uint32_t* part, uint32_t* scnt) {
   if (order && k <= 1024u) {
     // largest cluster first, so that the longest ordered sums start first
-    for (uint32_t c = threadIdx.x; c < k; c += blockDim.x) scnt[c] = counts[c];
+    for (uint32_t c = threadIdx.x; c < k; c += blockDim.x) scnt[c] = __ldcg(counts + c);
     __syncthreads();
     for (uint32_t c = threadIdx.x; c < k; c += blockDim.x) {
       const uint32_t v = scnt[c];
@@ -876,7 +966,7 @@ __global__ void cluster_scan_kernel(const uint32_t* __restrict__ counts, uint32_
   const uint32_t per = (k + blockDim.x - 1) / blockDim.x;
   const uint32_t b = threadIdx.x * per, e = min(k, b + per);
   uint32_t s = 0;
-  for (uint32_t i = b; i < e; ++i) s += counts[i];
+  for (uint32_t i = b; i < e; ++i) s += __ldcg(counts + i);
   // exclusive block scan of s: warp shuffles, then the warp totals
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   uint32_t x = s;
@@ -899,9 +989,72 @@ __global__ void cluster_scan_kernel(const uint32_t* __restrict__ counts, uint32_
   }
   __syncthreads();
   uint32_t acc = x - s + (wid > 0 ? part[wid - 1] : 0u);
-  for (uint32_t i = b; i < e; ++i) { cstart[i] = acc; acc += counts[i]; }
+  for (uint32_t i = b; i < e; ++i) { cstart[i] = acc; acc += __ldcg(counts + i); }
   if (e == k && b < e) cstart[k] = acc;
   if (k == 0 && threadIdx.x == 0) cstart[0] = 0;
+}
+
+// One warp per cluster: exclusive scan over its segments, total -> counts.
+// With cstart, the block that finishes last (a ticket in DevState) then runs
+// the cluster scan, which saves a dependent launch.  At most 512 threads per
+// block (80 registers a thread).
+__global__ void __launch_bounds__(512) seg_scan_kernel(uint32_t* __restrict__ seghist, uint32_t k, uint32_t nseg,
+                                uint32_t* __restrict__ counts, DevState* st, uint32_t* __restrict__ cstart,
+                                uint32_t* __restrict__ order) {
+  griddep_wait();
+  if (st->done) return;
+  const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c < k) {
+    uint32_t* h = seghist + (uint64_t)c * nseg;
+    uint32_t carry = 0;
+    // groups of 32 coalesced chunks: every load of a group is issued before the
+    // scans that use them
+    for (uint32_t g = 0; g < nseg; g += 32u * 32u) {
+      uint32_t v[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const uint32_t i = g + (uint32_t)q * 32u + (uint32_t)lane;
+        v[q] = (i < nseg) ? h[i] : 0u;
+      }
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const uint32_t i = g + (uint32_t)q * 32u + (uint32_t)lane;
+        uint32_t x = v[q];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x += y;
+        }
+        if (i < nseg) h[i] = carry + x - v[q];
+        carry += __shfl_sync(0xffffffffu, x, 31);
+      }
+    }
+    if (lane == 0) counts[c] = carry;
+  }
+  if (!cstart) return;
+  __shared__ uint32_t part[32];
+  __shared__ uint32_t scnt[1024];
+  __shared__ int is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = (atomicAdd(&st->scan_ticket, 1u) == gridDim.x - 1u) ? 1 : 0;
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  cluster_scan_block(counts, k, cstart, order, part, scnt);
+  if (threadIdx.x == 0) reinterpret_cast<volatile DevState*>(st)->scan_ticket = 0u;
+}
+
+// Single block: cluster_scan_block as a kernel of its own.
+__global__ void cluster_scan_kernel(const uint32_t* __restrict__ counts, uint32_t k,
+                                    uint32_t* __restrict__ cstart, DevState* st,
+                                    uint32_t* __restrict__ order) {
+  griddep_wait();
+  if (st->done) return;
+  __shared__ uint32_t part[32];
+  __shared__ uint32_t scnt[1024];
+  cluster_scan_block(counts, k, cstart, order, part, scnt);
 }
 
 // One warp per segment: stable scatter of row ids into perm.
@@ -909,6 +1062,7 @@ __global__ void seg_scatter_kernel(const uint32_t* __restrict__ labels, uint64_t
                                    uint32_t seg, uint32_t nseg, const uint32_t* __restrict__ seghist,
                                    const uint32_t* __restrict__ cstart,
                                    uint32_t* __restrict__ perm, DevState* st) {
+  griddep_wait();
   if (st->done) return;
   extern __shared__ uint32_t sh_pos[];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -974,9 +1128,6 @@ __device__ __forceinline__ void cp_async_4(void* smem, const void* gmem, uint32_
                "r"(src_bytes)
                : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 }  // namespace
 
 template <int VEC>
@@ -985,8 +1136,9 @@ update_sums_kernel(const float* __restrict__ X, const uint32_t* __restrict__ per
                    const uint32_t* __restrict__ cstart, uint32_t d, uint32_t k,
                    const float* __restrict__ C, float* __restrict__ Cn,
                    float* __restrict__ dsq, double* __restrict__ objpart, DevState* st) {
+  griddep_wait();
   if (st && st->done) return;
-  extern __shared__ __align__(16) float ring[];   // [UPD_STAGES][UPD_ROWS][32 * VEC]
+  extern __shared__ __align__(128) float ring[];   // [UPD_STAGES][UPD_ROWS][32 * VEC]
   constexpr uint32_t W = 32u * VEC;
   const uint32_t nchunk = (d + W - 1) / W;
   const uint64_t gw = blockIdx.x;
@@ -1132,6 +1284,7 @@ update_sums_bulk_kernel(const float* __restrict__ X, const uint32_t* __restrict_
                         const float* __restrict__ C, float* __restrict__ Cn,
                         float* __restrict__ dsq, double* __restrict__ objpart, DevState* st,
                         const uint32_t* __restrict__ order) {
+  griddep_wait();
   if (st && st->done) return;
   extern __shared__ __align__(128) float ring[];        // [BLK_STAGES][BLK_ROWS][BLK_COLS]
   __shared__ __align__(8) uint64_t full[BLK_STAGES], empty[BLK_STAGES];
@@ -1297,8 +1450,8 @@ km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_
                              DevState* st, cudaStream_t s, const uint32_t* order) {
   if (d % 4 == 0 && reinterpret_cast<uintptr_t>(X) % 16 == 0) {
     const uint64_t ctas = (uint64_t)k * ((d + BLK_COLS - 1) / BLK_COLS);
-    update_sums_bulk_kernel<<<(unsigned)ctas, BLK_THREADS, BLK_SMEM, s>>>(
-        X, perm, cstart, d, k, C, Cn, dsq, objpart, st, order);
+    KM_CUDA_TRY(launch_pdl(update_sums_bulk_kernel, (unsigned)ctas, BLK_THREADS, BLK_SMEM, s, X, perm, cstart, d,
+                           k, C, Cn, dsq, objpart, st, order));
     KM_CUDA_TRY(cudaGetLastError());
     return KM_OK;
   }
@@ -1317,9 +1470,6 @@ km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_
 
 // One warp per cluster: reference shift test (float sum over j ascending, then
 // sqrtf(s) > tol, kmeans.cpp:190-200), FP64 move, FP64 objective of the
-// cluster, new ||c||^2 and BF16 copies; then C <- Cn.
-// One warp per cluster: reference shift test (float sum over j ascending, then
-// sqrtf(s) > tol, kmeans.cpp:190-200), FP64 move, FP64 objective of the
 // cluster, new ||c||^2 and BF16 copies; then C <- Cn.  The block that finishes
 // last (a ticket in DevState) then ends the iteration: deterministic
 // reductions over the clusters, the stop decision, counters for the next
@@ -1333,14 +1483,14 @@ finalize_kernel(const float* __restrict__ Cn, float* __restrict__ C,
                 __nv_bfloat16* __restrict__ Clo, float* __restrict__ Ct,
                 double* __restrict__ shift_c, double* __restrict__ obj_c,
                 DevState* st, LoopConsts lc) {
+  griddep_wait();
   if (st->done) return;
-  __shared__ float sterm[8][32];
   __shared__ double s_obj[256];
   __shared__ double s_sh[256];
   __shared__ float s_cm[256];
   __shared__ int is_last;
   const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   if (c < k) {
     const uint64_t base = (uint64_t)c * d;
     // Reference GPU rule (src/kernels/distances.cu:588-599): an empty cluster's
@@ -1348,19 +1498,47 @@ finalize_kernel(const float* __restrict__ Cn, float* __restrict__ C,
     // its column of Ct become +inf; its (zero) centroid row stays finite.
     const bool excl = empty_excl && counts[c] == 0u;
     double nrm = 0.0, mv = 0.0, ob = 0.0;
-    for (uint32_t j = lane; j < dp; j += 32) {
-      const float v = (j < d) ? Cn[base + j] : 0.0f;
-      if (j < d) {
-        nrm += (double)v * v;
-        const double t = (double)v - (double)C[base + j];
-        mv += t * t;
-        ob += objpart[base + j];
-        Ct[(uint64_t)j * k + c] = excl ? f_inf() : v;
+    float s = 0.0f;   // reference shift test: float sum of dsq over j ascending
+    // 128 columns per pass, j = j0 + lane + 32 q: all of the pass's loads are
+    // issued before its arithmetic; the ordered float sum takes the terms from
+    // the lanes by shuffle (j ascending), the FP64 sums keep each lane's order.
+    for (uint32_t j0 = 0; j0 < dp; j0 += 128) {
+      float v[4], co[4], dq[4];
+      double op[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t j = j0 + (uint32_t)lane + 32u * q;
+        const bool in = j < d;
+        v[q] = in ? Cn[base + j] : 0.0f;
+        co[q] = in ? C[base + j] : 0.0f;
+        dq[q] = in ? dsq[base + j] : 0.0f;
+        op[q] = in ? objpart[base + j] : 0.0;
       }
-      if (Cb) {
-        const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-        Cb[(uint64_t)c * dp + j] = hi;
-        if (Clo) Clo[(uint64_t)c * dp + j] = __float2bfloat16_rn(v - __bfloat162float(hi));
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t j = j0 + (uint32_t)lane + 32u * q;
+        if (j < d) {
+          nrm += (double)v[q] * v[q];
+          const double t = (double)v[q] - (double)co[q];
+          mv += t * t;
+          ob += op[q];
+          Ct[(uint64_t)j * k + c] = excl ? f_inf() : v[q];
+          C[base + j] = v[q];
+        }
+        if (Cb && j < dp) {
+          const __nv_bfloat16 hi = __float2bfloat16_rn(v[q]);
+          Cb[(uint64_t)c * dp + j] = hi;
+          if (Clo) Clo[(uint64_t)c * dp + j] = __float2bfloat16_rn(v[q] - __bfloat162float(hi));
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t jq = j0 + 32u * q;
+#pragma unroll
+        for (int l = 0; l < 32; ++l) {
+          const float tq = __shfl_sync(0xffffffffu, dq[q], l);
+          if (jq + (uint32_t)l < d) s = __fadd_rn(s, tq);
+        }
       }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -1368,26 +1546,12 @@ finalize_kernel(const float* __restrict__ Cn, float* __restrict__ C,
       mv += __shfl_xor_sync(0xffffffffu, mv, o);
       ob += __shfl_xor_sync(0xffffffffu, ob, o);
     }
-    // Reference shift test: float sum over j ascending.  Coalesced loads of 32
-    // terms into shared memory, summed in order by lane 0.
-    float s = 0.0f;
-    for (uint32_t j0 = 0; j0 < d; j0 += 32) {
-      sterm[wib][lane] = (j0 + (uint32_t)lane < d) ? dsq[base + j0 + lane] : 0.0f;
-      __syncwarp();
-      if (lane == 0) {
-        const uint32_t m = min(32u, d - j0);
-        for (uint32_t q = 0; q < m; ++q) s = __fadd_rn(s, sterm[wib][q]);
-      }
-      __syncwarp();
-    }
     if (lane == 0) {
       if (sqrtf(s) > tol) st->moved = 1u;
       cn2[c] = excl ? f_inf() : (float)nrm;
       shift_c[c] = sqrt(mv);
       obj_c[c] = ob;
     }
-    __syncwarp();
-    for (uint32_t j = lane; j < d; j += 32) C[base + j] = Cn[base + j];
   }
   // ---- last block: end of iteration ----
   __threadfence();

@@ -110,7 +110,7 @@ extern "C" km_status km_update_noalloc(const float* X_dev, const uint32_t* label
   KM_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(DevState), s));
   const unsigned hb = (nseg + wpb - 1) / wpb;
   seg_hist_kernel<<<hb, wpb * 32, smem, s>>>(labels_dev, n, k, seg, nseg, seghist, st);
-  seg_scan_kernel<<<(k * 32 + 255) / 256, 256, 0, s>>>(seghist, k, nseg, counts, st);
+  seg_scan_kernel<<<(k * 32 + 255) / 256, 256, 0, s>>>(seghist, k, nseg, counts, st, nullptr, nullptr);
   cluster_scan_kernel<<<1, 1024, 0, s>>>(counts, k, cstart, st, nullptr);
   seg_scatter_kernel<<<hb, wpb * 32, smem, s>>>(labels_dev, n, k, seg, nseg, seghist, cstart, perm, st);
   KM_CUDA_TRY(cudaGetLastError());

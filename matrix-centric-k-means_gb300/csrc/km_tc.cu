@@ -98,6 +98,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   constexpr bool ALO = MODE == TC_SPLIT3;      // point operand has a lo part
   constexpr bool BLO = MODE != TC_PLAIN;       // centroid operand has a lo part
   constexpr uint32_t UPK = ALO ? 2u : 1u;      // ring units per K block (hi, then lo)
+  griddep_wait();
   if (st->done) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -418,6 +419,7 @@ assign_tc_chunked_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_c
                          float* __restrict__ mindist, RefineQueues rq, float* __restrict__ Dout) {
   constexpr bool ALO = MODE == TC_SPLIT3;
   constexpr bool BLO = MODE != TC_PLAIN;
+  griddep_wait();
   if (st->done) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -822,13 +824,11 @@ void launch_mode(const TcPlan& pl, const CUtensorMap& tmA, const CUtensorMap& tm
                  uint32_t kp, TieBound tb, DevState* st, uint32_t* labels, float* mindist,
                  const RefineQueues& rq, float* Dout, cudaStream_t s) {
   if (pl.chunked)
-    assign_tc_chunked_kernel<MODE><<<pl.grid, TCC_THREADS, pl.smem, s>>>(
-        tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.NC, pl.KB, pl.stages, pl.T, tb, st, labels,
-        mindist, rq, Dout);
+    (void)launch_pdl(assign_tc_chunked_kernel<MODE>, pl.grid, TCC_THREADS, pl.smem, s, tmA, tmAlo, tmB, tmBlo, cn2,
+                     xn2, n, k, kp, pl.NC, pl.KB, pl.stages, pl.T, tb, st, labels, mindist, rq, Dout);
   else
-    assign_tc_kernel<MODE><<<pl.grid, TC_THREADS, pl.smem, s>>>(
-        tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.KB, pl.stages, pl.nalloc, tb, st, labels,
-        mindist, rq, Dout);
+    (void)launch_pdl(assign_tc_kernel<MODE>, pl.grid, TC_THREADS, pl.smem, s, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n,
+                     k, kp, pl.KB, pl.stages, pl.nalloc, tb, st, labels, mindist, rq, Dout);
 }
 }  // namespace
 
