@@ -574,10 +574,11 @@ refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, ui
 // range's entries in passes.  A pass takes the leading entries whose point
 // rows and candidate centroid rows fit RS_ROWS staged rows: the entries' point
 // rows at [0, ne), the pairs' centroid rows at [ne, ne + np), pair p on lane p.
-// The rows are copied by 16-byte cp.async, one row per instruction on
-// contiguous lanes (four 128-byte lines), RS_CH columns per round trip (all of
-// d when d <= RS_CH); the loads of the next pass's entries are issued before
-// the copies are waited on.  Every lane then runs the reference's ordered
+// The rows are copied by the TMA engine, one bulk copy per row issued by the
+// lane that owns the row, RS_CH columns per round trip (all of d when d <=
+// RS_CH), completing on the warp's mbarrier; the loads of the next pass's
+// entries are issued before the copies are waited on.  (16-byte cp.async per
+// lane, one row per instruction, spent most of the pass issuing the copies.)  Every lane then runs the reference's ordered
 // chain (float, j ascending, no contraction) from shared memory.  A lane that
 // loads its own rows straight from global memory touches up to 32 lines per
 // instruction, and the L1 wavefronts, not DRAM, then set the time.  The
@@ -586,10 +587,11 @@ refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, ui
 // provably holds the reference argmin over all k (tie_tau / tie_class).
 // FULL: the warp also re-scores the rows of its segments' full queue against
 // all k (full_rescore_group), so that one launch covers the whole refinement.
-constexpr int RS_WARPS = 4;
-constexpr int RS_ROWS = 32;              // staged rows per pass
+constexpr int RS_WARPS = 5;
+constexpr int RS_ROWS = 40;              // staged rows per pass (at most 32 pairs)
 constexpr uint32_t RS_CH = 128;          // staged columns per round trip
-constexpr int RS_BLOCKS_PER_SM = 3;
+constexpr int RS_BLOCKS_PER_SM = 2;
+constexpr uint64_t RS_WAIT_NS = 2000000000ull;   // bound of a wait for the warp's copies
 // Shared row stride in floats for chunks of ch columns, with (stride / 4) odd
 // so that float4 reads of eight consecutive rows cover the 32 banks.
 __host__ __device__ constexpr uint32_t rs_ld(uint32_t ch) { return ((ch + 4u) / 4u) % 2u ? ch + 4u : ch + 8u; }
@@ -603,9 +605,19 @@ refine_staged_kernel(const float* __restrict__ X, const float* __restrict__ C, c
   griddep_wait();
   if (st->done) return;
   extern __shared__ __align__(16) float rs_smem[];
+  __shared__ __align__(8) uint64_t rs_bar[RS_WARPS];
+  __shared__ int rs_no_abort[RS_WARPS];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const uint32_t ch = min(d, RS_CH), ld = rs_ld(ch);
   float* const stg = rs_smem + (size_t)wib * RS_ROWS * ld;
+  uint64_t* const bar = &rs_bar[wib];   // this warp's copies
+  if (lane == 0) {
+    mbar_init(bar, 1);
+    rs_no_abort[wib] = 0;
+    mbar_fence_init();
+  }
+  __syncwarp();
+  uint32_t ph = 0;   // parity of the barrier phase the next wait completes
   const uint64_t nranges = (rq.nseg + span - 1) / span;
   const uint64_t nw = (uint64_t)gridDim.x * RS_WARPS;
   uint32_t cand_rows = 0, full_rows = 0;
@@ -647,9 +659,10 @@ refine_staged_kernel(const float* __restrict__ X, const float* __restrict__ C, c
         if (lane >= o) incl += y;
       }
       // entries of this pass: the leading lanes whose rows (one point row per
-      // entry, one centroid row per pair) fit RS_ROWS (at least six, cl <= 4)
-      const uint32_t ne =
-          (uint32_t)__popc(__ballot_sync(0xffffffffu, has && (uint32_t)lane + 1u + incl <= (uint32_t)RS_ROWS));
+      // entry, one centroid row per pair) fit RS_ROWS and whose pairs fit the
+      // 32 lanes (at least eight entries, cl <= 4)
+      const uint32_t ne = (uint32_t)__popc(
+          __ballot_sync(0xffffffffu, has && incl <= 32u && (uint32_t)lane + 1u + incl <= (uint32_t)RS_ROWS));
       const uint32_t np = __shfl_sync(0xffffffffu, incl, (int)ne - 1);
       const uint32_t off = incl - cl;
       // pair p = lane: its entry e (the last entry lane with off <= p)
@@ -668,16 +681,25 @@ refine_staged_kernel(const float* __restrict__ X, const float* __restrict__ C, c
       const uint32_t q3 = __shfl_sync(0xffffffffu, en.c[3], (int)e);
       const uint32_t cand = m == 0 ? q0 : m == 1 ? q1 : m == 2 ? q2 : q3;   // meaningful for p < np
       const uint32_t nrows = ne + np;
-      // columns [j0, j0 + nc) of the pass's rows, one row per instruction
+      // Source rows of the staged rows: lane r holds staged row r (r < 32) and
+      // lane r - 32 holds staged row r >= 32 (16-byte aligned: d % 4 == 0).
+      const uint32_t crl = __shfl_sync(0xffffffffu, cand, (int)(((uint32_t)lane - ne) & 31u));
+      const uint32_t crh = __shfl_sync(0xffffffffu, cand, (int)(((uint32_t)lane + 32u - ne) & 31u));
+      const uint64_t srcl = (uint32_t)lane < ne ? reinterpret_cast<uint64_t>(X + (uint64_t)en.row * d)
+                                                : reinterpret_cast<uint64_t>(C + (uint64_t)crl * d);
+      const uint64_t srch = reinterpret_cast<uint64_t>(C + (uint64_t)crh * d);
+      // columns [j0, j0 + nc) of the pass's rows: one bulk copy per row (a
+      // multiple of 16 bytes between 16-byte aligned addresses)
       auto stage = [&](uint32_t j0) {
-        const uint32_t nc4 = min(ch, d - j0) / 4u;
-        for (uint32_t r = 0; r < nrows; ++r) {
-          const uint32_t xr = __shfl_sync(0xffffffffu, en.row, (int)(r & 31u));
-          const uint32_t cr = __shfl_sync(0xffffffffu, cand, (int)((r - ne) & 31u));
-          const float* src = r < ne ? X + (uint64_t)xr * d : C + (uint64_t)cr * d;
-          if ((uint32_t)lane < nc4) cp_async16_zfill(stg + r * ld + 4u * lane, src + j0 + 4u * lane, 16u);
-        }
-        cp_async_commit();
+        const uint32_t bytes = min(ch, d - j0) * 4u;
+        // Every earlier read of the rows has returned its value (the chain's
+        // sums went through the lane reduction) before any lane gets here.
+        if (lane == 0) mbar_arrive_expect_tx(bar, nrows * bytes);
+        __syncwarp();
+        if ((uint32_t)lane < nrows)
+          bulk_copy_g2s(stg + lane * ld, reinterpret_cast<const float*>(srcl) + j0, bytes, bar);
+        if ((uint32_t)lane + 32u < nrows)
+          bulk_copy_g2s(stg + (32u + lane) * ld, reinterpret_cast<const float*>(srch) + j0, bytes, bar);
       };
       stage(0);
       const uint32_t e0n = e0 + ne;
@@ -691,8 +713,15 @@ refine_staged_kernel(const float* __restrict__ X, const float* __restrict__ C, c
       };
       for (uint32_t j0 = 0; j0 < d; j0 += ch) {
         if (j0) stage(j0);
-        cp_async_wait<0>();
-        __syncwarp();
+        const bool okw = mbar_wait_bounded(bar, ph, &rs_no_abort[wib], RS_WAIT_NS);
+        ph ^= 1u;
+        if (!__all_sync(0xffffffffu, okw)) {
+          // copies that never landed: flag, give the ones in flight a bounded
+          // second wait, and end this warp (no block barrier follows)
+          if (lane == 0) atomicOr(&st->err, KM_DEVERR_TIMEOUT);
+          mbar_wait_bounded(bar, ph ^ 1u, &rs_no_abort[wib], RS_WAIT_NS);
+          return;
+        }
         if (p < np) {
           const float4* xs = reinterpret_cast<const float4*>(stg + e * ld);
           const float4* cs = reinterpret_cast<const float4*>(stg + (ne + p) * ld);
