@@ -174,6 +174,17 @@ struct Top3 {
     v1 = c1 ? v : v1;
     i1 = c1 ? i : i1;
   }
+  // Insertion when every index already held is below i (columns visited in
+  // ascending order): a tie keeps the earlier entry, so strict '<' gives the
+  // (v, i) order for finite values.
+  __device__ __forceinline__ void insert_asc(float v, uint32_t i) {
+    const bool c1 = v < v1, c2 = v < v2, c3 = v < v3;
+    v3 = c2 ? v2 : (c3 ? v : v3);
+    v2 = c1 ? v1 : (c2 ? v : v2);
+    i2 = c1 ? i1 : (c2 ? i : i2);
+    v1 = c1 ? v : v1;
+    i1 = c1 ? i : i1;
+  }
   __device__ __forceinline__ void merge(const Top3& o) {
     insert_nb(o.v1, o.i1);
     insert_nb(o.v2, o.i2);

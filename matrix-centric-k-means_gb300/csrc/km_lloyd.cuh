@@ -81,7 +81,8 @@ km_status launch_assign_tc(const TcPlan& pl, int mode, const CUtensorMap& tmA,
                            float* Dout, cudaStream_t s);
 
 km_status update_sums_prepare();
-// Shared-memory limits of the staged re-score kernels (once per process and device).
+// Shared-memory limits of the staged re-score and FP32 distance kernels (once
+// per process and device, before their first launch).
 km_status refine_prepare();
 // order (nullable): the clusters' processing order (largest first).
 km_status launch_update_sums(const float* X, const uint32_t* perm, const uint32_t* cstart, uint32_t d,

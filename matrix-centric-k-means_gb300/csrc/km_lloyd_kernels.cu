@@ -147,6 +147,9 @@ __global__ void prep_centroids_kernel(const float* __restrict__ C, uint32_t k, u
 // ---------------------------------------------------------------------------
 namespace {
 constexpr int SM_ = 128, SN_ = 128, SK_ = 16, SPAD = 4;
+// Dynamic shared memory of assign_f32_kernel: each thread's running top-3 of
+// its eight rows ([5][8][256] words: v1, v2, v3, i1, i2).
+constexpr size_t F32_TOP_SMEM = 5 * 8 * 256 * sizeof(float);
 }
 
 // Thread (tx, ty) of the 16 x 16 grid owns rows ty*8 .. ty*8+7 and the two
@@ -173,8 +176,24 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
   __shared__ float cns[SN_];
   __shared__ float bv1[SM_], bv2[SM_], bv3[SM_];
   __shared__ uint32_t bi1[SM_], bi2[SM_];
+  // Each thread's running top-3 of its eight rows over the column tiles so far.
+  // A thread visits its columns in ascending order (tx*4 + j, then 64 + tx*4 +
+  // j, tile by tile), so strict-order insertion keeps the lowest index on
+  // ties; the 16 lanes of a row are merged under the (v, i) order once, after
+  // the last tile.
+  extern __shared__ float f32_top[];
+  float* const tv1 = f32_top;
+  float* const tv2 = f32_top + 8 * 256;
+  float* const tv3 = f32_top + 16 * 256;
+  uint32_t* const ti1 = reinterpret_cast<uint32_t*>(f32_top + 24 * 256);
+  uint32_t* const ti2 = reinterpret_cast<uint32_t*>(f32_top + 32 * 256);
 
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    tv1[i * 256 + tid] = tv2[i * 256 + tid] = tv3[i * 256 + tid] = f_inf();
+    ti1[i * 256 + tid] = ti2[i * 256 + tid] = 0xffffffffu;
+  }
   const uint64_t m0 = (uint64_t)blockIdx.x * SM_;
   if (tid < SM_) {
     bv1[tid] = bv2[tid] = bv3[tid] = f_inf();
@@ -272,31 +291,38 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
       __syncthreads();
     }
 
-    // Epilogue: v = ||c||^2 - 2 x.c, top-3 per row across the 16 lanes of a row.
+    // Epilogue: v = ||c||^2 - 2 x.c into the thread's running top-3 per row.
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int r = ty * 8 + i;
       const uint64_t row = m0 + r;                      // Dout is written in direct mode only
+      const int o = i * 256 + tid;
       Top3 t;
-      t.init();
+      t.v1 = tv1[o]; t.v2 = tv2[o]; t.v3 = tv3[o]; t.i1 = ti1[o]; t.i2 = ti2[o];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const uint32_t cl = (j < 4) ? (uint32_t)(tx * 4 + j) : (uint32_t)(64 + tx * 4 + j - 4);
         const uint32_t col = c0 + cl;
         const float v = fmaf(-2.0f, acc[i][j], cns[cl]);
         if (Dout && row < n && col < k) Dout[row * k + col] = v + xn2[row];
-        if (col < k) t.insert_nb(v, col);
+        if (col < k) t.insert_asc(v, col);
       }
-      t.shfl_merge_xor(8);
-      t.shfl_merge_xor(4);
-      t.shfl_merge_xor(2);
-      t.shfl_merge_xor(1);
-      if (tx == 0) {
-        Top3 b;
-        b.v1 = bv1[r]; b.v2 = bv2[r]; b.v3 = bv3[r]; b.i1 = bi1[r]; b.i2 = bi2[r];
-        b.merge(t);
-        bv1[r] = b.v1; bv2[r] = b.v2; bv3[r] = b.v3; bi1[r] = b.i1; bi2[r] = b.i2;
-      }
+      tv1[o] = t.v1; tv2[o] = t.v2; tv3[o] = t.v3; ti1[o] = t.i1; ti2[o] = t.i2;
+    }
+  }
+  // the 16 lanes of each row, merged under the (v, i) order
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int r = ty * 8 + i;
+    const int o = i * 256 + tid;
+    Top3 t;
+    t.v1 = tv1[o]; t.v2 = tv2[o]; t.v3 = tv3[o]; t.i1 = ti1[o]; t.i2 = ti2[o];
+    t.shfl_merge_xor(8);
+    t.shfl_merge_xor(4);
+    t.shfl_merge_xor(2);
+    t.shfl_merge_xor(1);
+    if (tx == 0) {
+      bv1[r] = t.v1; bv2[r] = t.v2; bv3[r] = t.v3; bi1[r] = t.i1; bi2[r] = t.i2;
     }
   }
   __syncthreads();
@@ -329,10 +355,10 @@ km_status launch_assign_f32(const float* X, const float* C, const float* cn2, co
   const bool v4 = (d % 4 == 0) && (reinterpret_cast<uintptr_t>(X) % 16 == 0) &&
                   (reinterpret_cast<uintptr_t>(C) % 16 == 0);
   if (v4)
-    assign_f32_kernel<true><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
+    assign_f32_kernel<true><<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
                                                    rq, Dout, nullptr, nullptr);
   else
-    assign_f32_kernel<false><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
+    assign_f32_kernel<false><<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
                                                     rq, Dout, nullptr, nullptr);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
@@ -869,6 +895,11 @@ refine_wide_kernel(const float* __restrict__ X, const float* __restrict__ C, uin
 }
 
 km_status refine_prepare() {
+  // assign_f32_kernel: 37 KB static + F32_TOP_SMEM dynamic is above the default 48 KB
+  KM_CUDA_TRY(cudaFuncSetAttribute(assign_f32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)F32_TOP_SMEM));
+  KM_CUDA_TRY(cudaFuncSetAttribute(assign_f32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)F32_TOP_SMEM));
   KM_CUDA_TRY(cudaFuncSetAttribute(refine_staged_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)RS_SMEM_MAX));
   KM_CUDA_TRY(cudaFuncSetAttribute(refine_staged_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -920,10 +951,10 @@ km_status launch_refine_gemm(bool v4, int num_sms, const float* X, const float* 
   const unsigned blocks = (unsigned)((n + SM_ - 1) / SM_);
   const bool gv4 = v4 && (reinterpret_cast<uintptr_t>(C) % 16 == 0);
   if (gv4)
-    assign_f32_kernel<true><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
+    assign_f32_kernel<true><<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
                                                    rq2, nullptr, fidx, nfull);
   else
-    assign_f32_kernel<false><<<blocks, 256, 0, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
+    assign_f32_kernel<false><<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
                                                     rq2, nullptr, fidx, nfull);
   launch_refine_cands(v4, num_sms, X, C, d, st, rq2, labels, mindist, false, s);
   refine_full_kernel<<<num_sms * 4, 256, 0, s>>>(X, Ct, d, k, st, rq2, labels, mindist, false);
