@@ -148,8 +148,12 @@ __global__ void prep_centroids_kernel(const float* __restrict__ C, uint32_t k, u
 namespace {
 constexpr int SM_ = 128, SN_ = 128, SK_ = 16, SPAD = 4;
 // Dynamic shared memory of assign_f32_kernel: each thread's running top-3 of
-// its eight rows ([5][8][256] words: v1, v2, v3, i1, i2).
-constexpr size_t F32_TOP_SMEM = 5 * 8 * 256 * sizeof(float);
+// its eight rows, five arrays (v1, v2, v3, i1, i2) of [128 rows][F32_TOP_LD]
+// words, lane tx of a row at column tx.  The stride 18 keeps the epilogue's
+// accesses (two rows 8 apart per warp) conflict-free and the final per-row
+// merge two-way at most.
+constexpr int F32_TOP_LD = 18;
+constexpr size_t F32_TOP_SMEM = 5 * 128 * F32_TOP_LD * sizeof(float);
 }
 
 // Thread (tx, ty) of the 16 x 16 grid owns rows ty*8 .. ty*8+7 and the two
@@ -174,30 +178,28 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
   __shared__ __align__(16) float As[2][SK_][SM_ + SPAD];
   __shared__ __align__(16) float Bs[2][SK_][SN_ + SPAD];
   __shared__ float cns[SN_];
-  __shared__ float bv1[SM_], bv2[SM_], bv3[SM_];
-  __shared__ uint32_t bi1[SM_], bi2[SM_];
   // Each thread's running top-3 of its eight rows over the column tiles so far.
   // A thread visits its columns in ascending order (tx*4 + j, then 64 + tx*4 +
   // j, tile by tile), so strict-order insertion keeps the lowest index on
-  // ties; the 16 lanes of a row are merged under the (v, i) order once, after
-  // the last tile.
+  // ties; after the last tile one thread per row merges the row's 16 lists
+  // under the (v, i) order.
   extern __shared__ float f32_top[];
+  constexpr int TA = SM_ * F32_TOP_LD;
   float* const tv1 = f32_top;
-  float* const tv2 = f32_top + 8 * 256;
-  float* const tv3 = f32_top + 16 * 256;
-  uint32_t* const ti1 = reinterpret_cast<uint32_t*>(f32_top + 24 * 256);
-  uint32_t* const ti2 = reinterpret_cast<uint32_t*>(f32_top + 32 * 256);
+  float* const tv2 = f32_top + TA;
+  float* const tv3 = f32_top + 2 * TA;
+  uint32_t* const ti1 = reinterpret_cast<uint32_t*>(f32_top + 3 * TA);
+  uint32_t* const ti2 = reinterpret_cast<uint32_t*>(f32_top + 4 * TA);
 
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    tv1[i * 256 + tid] = tv2[i * 256 + tid] = tv3[i * 256 + tid] = f_inf();
-    ti1[i * 256 + tid] = ti2[i * 256 + tid] = 0xffffffffu;
+    const int o = (ty * 8 + i) * F32_TOP_LD + tx;
+    tv1[o] = tv2[o] = tv3[o] = f_inf();
+    ti1[o] = ti2[o] = 0xffffffffu;
   }
   const uint64_t m0 = (uint64_t)blockIdx.x * SM_;
   if (tid < SM_) {
-    bv1[tid] = bv2[tid] = bv3[tid] = f_inf();
-    bi1[tid] = bi2[tid] = 0xffffffffu;
     const uint64_t li = m0 + tid;
     rmap[tid] = ridx ? (li < n_log ? ridx[li] : 0u) : (uint32_t)li;
   }
@@ -296,7 +298,7 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
     for (int i = 0; i < 8; ++i) {
       const int r = ty * 8 + i;
       const uint64_t row = m0 + r;                      // Dout is written in direct mode only
-      const int o = i * 256 + tid;
+      const int o = r * F32_TOP_LD + tx;
       Top3 t;
       t.v1 = tv1[o]; t.v2 = tv2[o]; t.v3 = tv3[o]; t.i1 = ti1[o]; t.i2 = ti2[o];
 #pragma unroll
@@ -310,37 +312,31 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
       tv1[o] = t.v1; tv2[o] = t.v2; tv3[o] = t.v3; ti1[o] = t.i1; ti2[o] = t.i2;
     }
   }
-  // the 16 lanes of each row, merged under the (v, i) order
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int r = ty * 8 + i;
-    const int o = i * 256 + tid;
-    Top3 t;
-    t.v1 = tv1[o]; t.v2 = tv2[o]; t.v3 = tv3[o]; t.i1 = ti1[o]; t.i2 = ti2[o];
-    t.shfl_merge_xor(8);
-    t.shfl_merge_xor(4);
-    t.shfl_merge_xor(2);
-    t.shfl_merge_xor(1);
-    if (tx == 0) {
-      bv1[r] = t.v1; bv2[r] = t.v2; bv3[r] = t.v3; bi1[r] = t.i1; bi2[r] = t.i2;
-    }
-  }
   __syncthreads();
 
-  // Classify rows (one thread per row) and queue near ties.
+  // One thread per row: merge the row's 16 lists, classify, queue near ties.
   if (tid < SM_) {
+    Top3 b;
+    b.init();
+#pragma unroll 4
+    for (int l = 0; l < 16; ++l) {
+      const int o = tid * F32_TOP_LD + l;
+      Top3 u;
+      u.v1 = tv1[o]; u.v2 = tv2[o]; u.v3 = tv3[o]; u.i1 = ti1[o]; u.i2 = ti2[o];
+      b.merge(u);
+    }
     const uint64_t li = m0 + tid;
     const bool valid = li < n_log;
     const uint64_t row = rmap[tid];
     int cls = 0;
-    uint32_t i1 = bi1[tid] == 0xffffffffu ? 0u : bi1[tid];
+    uint32_t i1 = b.i1 == 0xffffffffu ? 0u : b.i1;
     if (valid) {
       const float cn1 = sqrtf(fmaxf(cn2[i1], 0.0f));
-      cls = tie_class(xn2[row], bv1[tid], bv2[tid], bv3[tid], cn1, st->cmax, tb);
+      cls = tie_class(xn2[row], b.v1, b.v2, b.v3, cn1, st->cmax, tb);
       labels[row] = i1;
-      if (mindist) mindist[row] = bv1[tid] + xn2[row];
+      if (mindist) mindist[row] = b.v1 + xn2[row];
     }
-    RefineEntry e{(uint32_t)row, 2u, {i1, bi2[tid], 0u, 0u}};
+    RefineEntry e{(uint32_t)row, 2u, {i1, b.i2, 0u, 0u}};
     const uint64_t seg = li >> 5;
     seg_push(rq.cand, rq.ccnt, seg, valid && cls == 1, e);
     seg_push(rq.full, rq.fcnt, seg, valid && cls == 2, (uint32_t)row);
