@@ -42,6 +42,7 @@ N, D, K = 1_048_576, 128, 256
 BLOBS, LO, HI, SIGMA, DATA_SEED = 256, -10.0, 10.0, 1.0, 1000
 KM_SEED, TOL = 0, 1e-4
 E2E_ITERS = 20          # iterations of the end-to-end fit (one H2D of X per fit)
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12   # nominal FP32 FMA rate (80.5 TFLOP/s)
 METRIC = "iters/s (n=1M,d=128,k=256): BF16-TC vs FP32 plain at equal labels; % of peak"
 
 
@@ -373,7 +374,13 @@ def ours_arm(args, rank, world):
         "data": "synthetic",
         "config": bench_config(world),
         "precision": args.precision,
-        "fp32_plain": {"value": fp32_ips, "unit": "iters/s", "stages_ms": stages32},
+        "fp32_plain": {"value": fp32_ips, "unit": "iters/s", "stages_ms": stages32,
+                       # the FP32 distance kernel (stage 0) on 2nkd FLOP against the nominal FP32 rate
+                       "distance_tflops": (2.0 * N * K * D / (stages32[0] * 1e-3) / 1e12) if stages32 else None,
+                       "distance_frac_of_nominal": (2.0 * N * K * D / (stages32[0] * 1e-3) / 1e12 / FP32_NOMINAL_TFLOPS)
+                       if stages32 else None,
+                       "nominal_tflops": FP32_NOMINAL_TFLOPS,
+                       "nominal_source": "152 SMs x 128 FP32 lanes x 2 FLOP x 2.07 GHz; no measured FP32 figure"},
         "other_tc_forms": {q: {"value": timing[q]["iters"] / (timing[q]["ms_loop"] / 1000.0), "unit": "iters/s",
                                "label_agreement_vs_fp32": float((labels[q] == labels["fp32"]).mean()),
                                "refined_rows_per_iter": timing[q]["refined"] / max(1, timing[q]["iters"])}

@@ -160,8 +160,9 @@ constexpr size_t F32_TOP_SMEM = 5 * 128 * F32_TOP_LD * sizeof(float);
 // column quads tx*4 .. tx*4+3 and 64 + tx*4 .. +3 of the 128 x 128 tile: the
 // quarter-warps' 16-byte centroid loads from shared memory then cover 128
 // contiguous bytes (no bank conflicts), and two CTAs fit an SM.
-template <bool V4>
-__global__ void __launch_bounds__(256, 2)
+// DOUT (distance-matrix output): one CTA per SM, so that its stores do not spill.
+template <bool V4, bool DOUT>
+__global__ void __launch_bounds__(256, DOUT ? 1 : 2)
 assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
                   const float* __restrict__ cn2, const float* __restrict__ xn2, uint64_t n,
                   uint32_t d, uint32_t k, TieBound tb, DevState* st,
@@ -306,8 +307,10 @@ assign_f32_kernel(const float* __restrict__ X, const float* __restrict__ C,
         const uint32_t cl = (j < 4) ? (uint32_t)(tx * 4 + j) : (uint32_t)(64 + tx * 4 + j - 4);
         const uint32_t col = c0 + cl;
         const float v = fmaf(-2.0f, acc[i][j], cns[cl]);
-        if (Dout && row < n && col < k) Dout[row * k + col] = v + xn2[row];
-        if (col < k) t.insert_asc(v, col);
+        if (DOUT && row < n && col < k) Dout[row * k + col] = v + xn2[row];
+        // columns at or past k hold ||c||^2 = +inf, so v is +inf (or NaN)
+        // there and the strict insertion never takes them
+        t.insert_asc(v, col);
       }
       tv1[o] = t.v1; tv2[o] = t.v2; tv3[o] = t.v3; ti1[o] = t.i1; ti2[o] = t.i2;
     }
@@ -350,12 +353,10 @@ km_status launch_assign_f32(const float* X, const float* C, const float* cn2, co
   const unsigned blocks = (unsigned)((n + SM_ - 1) / SM_);
   const bool v4 = (d % 4 == 0) && (reinterpret_cast<uintptr_t>(X) % 16 == 0) &&
                   (reinterpret_cast<uintptr_t>(C) % 16 == 0);
-  if (v4)
-    assign_f32_kernel<true><<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
-                                                   rq, Dout, nullptr, nullptr);
-  else
-    assign_f32_kernel<false><<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist,
-                                                    rq, Dout, nullptr, nullptr);
+  auto kern = v4 ? (Dout ? assign_f32_kernel<true, true> : assign_f32_kernel<true, false>)
+                 : (Dout ? assign_f32_kernel<false, true> : assign_f32_kernel<false, false>);
+  kern<<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb, st, labels, mindist, rq, Dout, nullptr,
+                                         nullptr);
   KM_CUDA_TRY(cudaGetLastError());
   return KM_OK;
 }
@@ -892,10 +893,9 @@ refine_wide_kernel(const float* __restrict__ X, const float* __restrict__ C, uin
 
 km_status refine_prepare() {
   // assign_f32_kernel: 37 KB static + F32_TOP_SMEM dynamic is above the default 48 KB
-  KM_CUDA_TRY(cudaFuncSetAttribute(assign_f32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)F32_TOP_SMEM));
-  KM_CUDA_TRY(cudaFuncSetAttribute(assign_f32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)F32_TOP_SMEM));
+  for (auto kern : {assign_f32_kernel<true, true>, assign_f32_kernel<true, false>, assign_f32_kernel<false, true>,
+                    assign_f32_kernel<false, false>})
+    KM_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)F32_TOP_SMEM));
   KM_CUDA_TRY(cudaFuncSetAttribute(refine_staged_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)RS_SMEM_MAX));
   KM_CUDA_TRY(cudaFuncSetAttribute(refine_staged_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -947,10 +947,10 @@ km_status launch_refine_gemm(bool v4, int num_sms, const float* X, const float* 
   const unsigned blocks = (unsigned)((n + SM_ - 1) / SM_);
   const bool gv4 = v4 && (reinterpret_cast<uintptr_t>(C) % 16 == 0);
   if (gv4)
-    assign_f32_kernel<true><<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
+    assign_f32_kernel<true, false><<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
                                                    rq2, nullptr, fidx, nfull);
   else
-    assign_f32_kernel<false><<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
+    assign_f32_kernel<false, false><<<blocks, 256, F32_TOP_SMEM, s>>>(X, C, cn2, xn2, n, d, k, tb32, st, labels, mindist,
                                                     rq2, nullptr, fidx, nfull);
   launch_refine_cands(v4, num_sms, X, C, d, st, rq2, labels, mindist, false, s);
   refine_full_kernel<<<num_sms * 4, 256, 0, s>>>(X, Ct, d, k, st, rq2, labels, mindist, false);
