@@ -87,7 +87,9 @@ __device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, uint32_t* r) 
       : "memory");
 }
 
-template <int MODE>
+// DOUT: the distance-matrix output (km_distances); a template parameter so that
+// the assignment-only instance carries none of its code or registers.
+template <int MODE, bool DOUT>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
                  const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo,
@@ -326,7 +328,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
         }
         ghi[g] = ((p0 | p1) | (p2 | p3)) &
                  (nval >= 64u ? 0xffffffffu : (nval > 32u ? ((1u << (nval - 32u)) - 1u) : 0u));
-        if (Dout && valid) {
+        if (DOUT && valid) {
 #pragma unroll
           for (int j = 0; j < 64; ++j)
             if ((uint32_t)j < nval) Dout[row * k + cg + j] = __uint_as_float(acc[j]) + x2;
@@ -813,8 +815,12 @@ template <int MODE>
 km_status set_attr_mode(const TcPlan& pl) {
   if (pl.chunked)
     KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_chunked_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
-  else
-    KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+  else {
+    KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_kernel<MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)pl.smem));
+    KM_CUDA_TRY(cudaFuncSetAttribute(assign_tc_kernel<MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)pl.smem));
+  }
   return KM_OK;
 }
 
@@ -827,8 +833,9 @@ void launch_mode(const TcPlan& pl, const CUtensorMap& tmA, const CUtensorMap& tm
     (void)launch_pdl(assign_tc_chunked_kernel<MODE>, pl.grid, TCC_THREADS, pl.smem, s, tmA, tmAlo, tmB, tmBlo, cn2,
                      xn2, n, k, kp, pl.NC, pl.KB, pl.stages, pl.T, tb, st, labels, mindist, rq, Dout);
   else
-    (void)launch_pdl(assign_tc_kernel<MODE>, pl.grid, TC_THREADS, pl.smem, s, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n,
-                     k, kp, pl.KB, pl.stages, pl.nalloc, tb, st, labels, mindist, rq, Dout);
+    (void)launch_pdl(Dout ? assign_tc_kernel<MODE, true> : assign_tc_kernel<MODE, false>, pl.grid, TC_THREADS,
+                     pl.smem, s, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.KB, pl.stages, pl.nalloc, tb, st,
+                     labels, mindist, rq, Dout);
 }
 }  // namespace
 
