@@ -608,8 +608,8 @@ refine_full_kernel(const float* __restrict__ X, const float* __restrict__ Ct, ui
 // entry's lane picks the smallest distance over its candidates in ascending
 // index order with a strict '<' (lowest index on ties).  The candidate set
 // provably holds the reference argmin over all k (tie_tau / tie_class).
-// FULL: the warp also re-scores the rows of its segments' full queue against
-// all k (full_rescore_group), so that one launch covers the whole refinement.
+// FULL: the grid's warps then re-score the full queue against all k
+// (full_rescore_group), so that one launch covers the whole refinement.
 constexpr int RS_WARPS = 5;
 constexpr int RS_ROWS = 40;              // staged rows per pass (at most 32 pairs)
 constexpr uint32_t RS_CH = 128;          // staged columns per round trip
@@ -648,7 +648,6 @@ refine_staged_kernel(const float* __restrict__ X, const float* __restrict__ C, c
     const uint64_t seg0 = rg * span;
     const bool segok = (uint32_t)lane < span && seg0 + (uint64_t)lane < rq.nseg;
     const uint32_t c = segok ? rq.ccnt[seg0 + lane] : 0u;
-    const uint32_t fc = (FULL && segok) ? rq.fcnt[seg0 + lane] : 0u;
     uint32_t pre = c;   // inclusive prefix of the segment counts over the lanes
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -775,13 +774,24 @@ refine_staged_kernel(const float* __restrict__ X, const float* __restrict__ C, c
       en = enn;
       e0 = e0n;
     }
-    if (FULL) {
-      for (uint32_t q = 0; q < span; ++q) {
-        const uint32_t cnt = __shfl_sync(0xffffffffu, fc, (int)q);
+  }
+  if (FULL) {
+    // The full queue, interleaved over every warp of the grid as in
+    // refine_full_kernel (its rows can be many and bunched: e.g. the FP32 pass
+    // at very large k); 32 segment counts per load, only non-empty ones visited.
+    for (uint64_t g0 = (uint64_t)blockIdx.x * RS_WARPS + wib; g0 < rq.nseg; g0 += nw * 32) {
+      const uint64_t sgl = g0 + (uint64_t)lane * nw;
+      const uint32_t fl = (sgl < rq.nseg) ? rq.fcnt[sgl] : 0u;
+      uint32_t nz = __ballot_sync(0xffffffffu, fl != 0u);
+      while (nz) {
+        const int sl = __ffs(nz) - 1;
+        nz &= nz - 1u;
+        const uint64_t seg = g0 + (uint64_t)sl * nw;
+        const uint32_t cnt = __shfl_sync(0xffffffffu, fl, sl);
         full_rows += cnt;
         for (uint32_t f0 = 0; f0 < cnt; f0 += FULL_ROWS)
-          full_rescore_group(X, Ct, d, k, rq.full + (seg0 + (uint64_t)q) * 32 + f0,
-                             min(cnt - f0, (uint32_t)FULL_ROWS), labels, mindist);
+          full_rescore_group(X, Ct, d, k, rq.full + seg * 32 + f0, min(cnt - f0, (uint32_t)FULL_ROWS), labels,
+                             mindist);
       }
     }
   }

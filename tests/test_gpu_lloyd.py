@@ -100,6 +100,35 @@ def test_assign_near_ties(km, gpu, prec):
 
 
 @pytest.mark.parametrize("prec", PRECISIONS)
+@pytest.mark.parametrize("d", [4, 100, 132, 260])
+def test_assign_dense_queue_shapes(km, gpu, prec, d):
+    """Centroids in groups of 2..6 near-duplicates and points at the groups'
+    centres: almost every row is queued, many with 3..4 candidates (the staged
+    re-score's passes hit their row and pair limits) and the groups of 5..6
+    send rows to the full re-score.  d = 4, 100, 132, 260 cover a chunk of
+    fewer than 128 columns, a padded shared-memory row stride, and two or
+    three 128-column chunks per pass.  Labels must equal the reference
+    formula's."""
+    import torch
+    rng = np.random.default_rng(11 + d)
+    sizes = [2, 3, 4, 5, 6, 2, 3, 4, 6, 5, 2, 4]
+    base = rng.standard_normal((len(sizes), d)).astype(np.float32) * 4
+    cs, owner = [], []
+    for g, m in enumerate(sizes):
+        for _ in range(m):
+            cs.append(base[g] + rng.standard_normal(d).astype(np.float32) * 1e-5)
+            owner.append(g)
+    Cc = np.stack(cs).astype(np.float32)
+    n = 9000
+    grp = rng.integers(0, len(sizes), n)
+    X = (base[grp] + rng.standard_normal((n, d)).astype(np.float32) * 1e-3).astype(np.float32)
+    lab_o, _ = helpers.orc_assign(X, Cc)
+    lab, _, refined = km.assign(torch.from_numpy(X).to(gpu), torch.from_numpy(Cc).to(gpu), precision=prec)
+    np.testing.assert_array_equal(lab.cpu().numpy().astype(np.uint32), lab_o)
+    assert refined > n // 2
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
 @pytest.mark.parametrize("shape", [(3000, 96, 200), (2000, 64, 700)])
 def test_distances_vs_torch_fp32(km, gpu, prec, shape):
     """The fast-path distance stage against a plain PyTorch fp32 reference
