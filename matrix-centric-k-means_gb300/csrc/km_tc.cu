@@ -44,9 +44,14 @@ namespace km {
 
 namespace {
 
-constexpr int TC_SETS = 3;                            // k <= 256 kernel: epilogue sets of four warps
-constexpr int TC_EPI_WARPS = 4 * TC_SETS;
-constexpr int TC_THREADS = 32 * (4 + TC_EPI_WARPS);
+// Epilogue sets of four warps in the k <= 256 kernel, by form: the split
+// forms (two or three MMAs per K step) keep pace with two sets, whose warps then
+// get 168 registers (no spill); the single-BF16 form, with a third of the MMA
+// work per tile, is faster with three (128 registers).  Measured at n = 1M,
+// d = 128, k = 256: split-BF16x3 distance 0.150 ms with two sets, 0.153 with
+// three; single-BF16 iterations 3322 it/s with two sets, 3476 with three.
+__host__ __device__ constexpr int tc_sets(int mode) { return mode == TC_PLAIN ? 3 : 2; }
+__host__ __device__ constexpr int tc_threads(int mode) { return 32 * (4 + 4 * tc_sets(mode)); }
 constexpr int TCC_THREADS = 32 * (4 + 8);               // chunked kernel: two sets of four
 constexpr int TC_M = 128;
 constexpr uint64_t WAIT_NS = 2000000000ull;
@@ -55,16 +60,16 @@ constexpr uint32_t TC_MAX_UNITS = 16;
 // Suspend-time hint of the k <= 256 kernel's waits: a waiting warp sleeps
 // (until the phase completes) instead of spinning on issue slots the epilogue needs.
 constexpr uint32_t TC_HINT_NS = 1000;
-// Accumulator-full barriers: tile t (this CTA's t-th) completes tfull[t % TC_NTF].
-// Each of them is waited on by one epilogue set only (set t % TC_SETS), tile
-// after tile, so a parity wait never aliases another set's phase.
-constexpr int TC_NTF = 2 * TC_SETS;
+// Accumulator-full barriers: tile t (this CTA's t-th) completes tfull[t % NTF],
+// NTF = 2 x sets.  Each of them is waited on by one epilogue set only (set
+// t % sets), tile after tile, so a parity wait never aliases another set's phase.
+constexpr int TC_NTF_MAX = 6;
 
 struct TcSmem {
   uint64_t full[TC_MAX_UNITS];
   uint64_t empty[TC_MAX_UNITS];
   uint64_t bfull;
-  uint64_t tfull[TC_NTF];
+  uint64_t tfull[TC_NTF_MAX];
   uint64_t tempty[2];
   uint64_t tdone;
   uint32_t tmem_base;
@@ -90,7 +95,7 @@ __device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, uint32_t* r) 
 // DOUT: the distance-matrix output (km_distances); a template parameter so that
 // the assignment-only instance carries none of its code or registers.
 template <int MODE, bool DOUT>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(tc_threads(MODE), 1)
 assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
                  const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo,
                  const float* __restrict__ cn2, const float* __restrict__ xn2, uint64_t n,
@@ -100,6 +105,8 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   constexpr bool ALO = MODE == TC_SPLIT3;      // point operand has a lo part
   constexpr bool BLO = MODE != TC_PLAIN;       // centroid operand has a lo part
   constexpr uint32_t UPK = ALO ? 2u : 1u;      // ring units per K block (hi, then lo)
+  constexpr int SETS = tc_sets(MODE), NTF = 2 * SETS, EPI_WARPS = 4 * SETS;
+  static_assert(NTF <= TC_NTF_MAX, "accumulator-full barriers");
   griddep_wait();
   if (st->done) return;
   extern __shared__ uint8_t smem_raw[];
@@ -119,7 +126,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
   if (threadIdx.x == 0) {
     for (uint32_t s = 0; s < S; ++s) { mbar_init(&ts->full[s], 1); mbar_init(&ts->empty[s], 1); }
     mbar_init(&ts->bfull, 1);
-    for (int b = 0; b < TC_NTF; ++b) mbar_init(&ts->tfull[b], 1);
+    for (int b = 0; b < NTF; ++b) mbar_init(&ts->tfull[b], 1);
     for (int b = 0; b < 2; ++b) mbar_init(&ts->tempty[b], 4);
     mbar_init(&ts->tdone, 1);
     ts->abort = 0;
@@ -129,7 +136,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
     // centroid norms (padded with +inf by the host to a multiple of 64) into
     // shared memory, +inf up to 256
     const uint32_t kp64 = (kp + 63u) & ~63u;
-    for (uint32_t i = threadIdx.x - 128u; i < 256u; i += 32u * TC_EPI_WARPS)
+    for (uint32_t i = threadIdx.x - 128u; i < 256u; i += 32u * EPI_WARPS)
       xch->cn2[i] = i < kp64 ? cn2[i] : finf;
   }
   if (warp == 2) tmem_alloc(&ts->tmem_base, 2u * nalloc);
@@ -222,7 +229,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
           issued = true;
         }
         if (!ok) break;
-        tc_commit(&ts->tfull[t % TC_NTF]);
+        tc_commit(&ts->tfull[t % NTF]);
       }
       // All MMAs of this thread complete before teardown.
       if (issued) {
@@ -232,8 +239,8 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       }
     }
   } else if (warp >= 4) {
-    // Epilogue: TC_SETS sets of four warps; set s takes this CTA's tiles
-    // t = s, s + TC_SETS, ... (TMEM buffer t % 2), so several tiles are in the
+    // Epilogue: SETS sets of four warps; set s takes this CTA's tiles
+    // t = s, s + SETS, ... (TMEM buffer t % 2), so several tiles are in the
     // epilogue at once and no warp waits for another.  Warp w of a set owns
     // TMEM lanes (rows) 32*(w%4)..+31 and each thread sweeps its whole row in
     // groups of 64 columns: v = ||c||^2 - 2 acc, the group minimum, the running
@@ -248,7 +255,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
     const uint32_t r = (uint32_t)q * 32u + (uint32_t)lane;
     const uint32_t ng = (kp + 63u) / 64u;                // 64-column groups (1..4)
     const float* cns = xch->cn2;
-    for (uint64_t t = (uint64_t)set;; t += TC_SETS) {
+    for (uint64_t t = (uint64_t)set;; t += SETS) {
       const uint64_t tile = blockIdx.x + t * gridDim.x;
       if (tile >= ntiles) break;
       const uint32_t buf = (uint32_t)(t & 1u);
@@ -256,7 +263,7 @@ assign_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant_
       const bool valid = row < n;
       const float x2 = valid ? xn2[row] : 0.0f;
       const TauRow tr = tie_tau_row(x2, cmax, tb);
-      const bool okw = mbar_wait_bounded(&ts->tfull[t % TC_NTF], (uint32_t)((t / TC_NTF) & 1u), abort_flag,
+      const bool okw = mbar_wait_bounded(&ts->tfull[t % NTF], (uint32_t)((t / NTF) & 1u), abort_flag,
                                          WAIT_NS, TC_HINT_NS);
       if (!__all_sync(0xffffffffu, okw)) { if (lane == 0) fail(5); break; }
       tc_fence_after();
@@ -833,7 +840,7 @@ void launch_mode(const TcPlan& pl, const CUtensorMap& tmA, const CUtensorMap& tm
     (void)launch_pdl(assign_tc_chunked_kernel<MODE>, pl.grid, TCC_THREADS, pl.smem, s, tmA, tmAlo, tmB, tmBlo, cn2,
                      xn2, n, k, kp, pl.NC, pl.KB, pl.stages, pl.T, tb, st, labels, mindist, rq, Dout);
   else
-    (void)launch_pdl(Dout ? assign_tc_kernel<MODE, true> : assign_tc_kernel<MODE, false>, pl.grid, TC_THREADS,
+    (void)launch_pdl(Dout ? assign_tc_kernel<MODE, true> : assign_tc_kernel<MODE, false>, pl.grid, tc_threads(MODE),
                      pl.smem, s, tmA, tmAlo, tmB, tmBlo, cn2, xn2, n, k, kp, pl.KB, pl.stages, pl.nalloc, tb, st,
                      labels, mindist, rq, Dout);
 }
