@@ -861,9 +861,9 @@ def batch_arm(args):
 # (profiles/lloyd_iteration_n1M_d128_k256_launches.md; averages over the
 # launches of each arm).  Keys: (precision, stage).
 TRAFFIC = {
-    ("bf16x3", "distance+argmin"): 554.7e6,      # assign_tc_kernel<1>
-    ("bf16x3", "refine"): 43.9e6 + 0.2e6,        # refine_pairs_kernel + refine_full_kernel
-    ("bf16x3", "label sort"): 10.6e6,            # seg_hist + seg_scan + cluster_scan + seg_scatter
+    ("bf16x3", "distance+argmin"): 551.8e6,      # assign_tc_kernel<1, false>
+    ("bf16x3", "refine"): 44.0e6,                # refine_staged_kernel<true>
+    ("bf16x3", "label sort"): 10.6e6,            # seg_hist + seg_scan + seg_scatter
     ("bf16x3", "centroid sums"): 541.6e6,        # update_sums_bulk_kernel
     ("bf16x3", "finalize+control"): 0.7e6,
     ("bf16", "distance+argmin"): 283.1e6,        # assign_tc_kernel<0>
