@@ -362,7 +362,7 @@ km_status launch_assign_f32(const float* X, const float* C, const float* cn2, co
 }
 
 // Exact re-score of rows with 2..4 candidates, for rows that are not 16-byte
-// aligned or d % 4 != 0 (refine_pairs_kernel below is the vector path): four
+// aligned or d % 4 != 0 (refine_staged_kernel below is the vector path): four
 // lanes per row, one candidate per lane, the reference's CPU distance (float,
 // j ascending); smallest distance wins, lowest index on ties.  The candidate
 // set provably holds the reference argmin over all k (tie_tau / tie_class).
